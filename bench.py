@@ -1,0 +1,361 @@
+"""Benchmark of the FP64 pseudo-spectral step (two-layer QG, nx=ny=256,
+dt=3600 s: the config-2 physics) in simulated years per wall-clock hour.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One timed step = one call of the fused step over `--chunk` model steps
+(default 100) with the state resident in HBM; L2 is flushed (a 256 MB
+write) before every timed step.  Prints one JSON line on rank 0.
+
+--impl reference times the reference's own CPU kernel (pyqg/kernel.pyx,
+compiled by oracle/build_ref.py) on the host cores, falling back to the
+numpy oracle port when that module cannot be built.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+YEAR = 360 * 86400.0          # pyqg/tests/test_reference_solns.py:12
+METRIC = "sim-yr/hr, 1 GB300: nx64+learned closure vs nx256 plain at matched KE error"
+C2 = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
+          U2=0.0, rek=5.787e-7, filterfac=23.6)
+QUIET = dict(tavestart=1e30, taveint=1e30, log_level=0)
+
+
+def sim_yr_per_hr(model_steps, dt, seconds):
+    return (model_steps * dt / YEAR) / (seconds / 3600.0)
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.index),
+                     "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 2 + i and s[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the reference kernel (or the oracle port) on host cores
+# --------------------------------------------------------------------------
+def cpu_model_steps(nsteps, nx=256, dt=3600.0, seed=0, threads=None):
+    """Run `nsteps` config-2 steps on the CPU with the reference's compiled
+    kernel (kind 'reference') or the numpy oracle (kind 'port').
+    Returns (seconds, kind, cores)."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import pyqg_oracle as O
+    from pyqg_gb300.model import grid_constants, spectral_filter
+    from pyqg_gb300.qg_model import qg_inversion_matrix
+    threads = threads or 1
+    g = grid_constants(nx, nx, C2["L"], C2["L"])
+    F1 = C2["rd"] ** -2 / (1. + C2["delta"])
+    F2 = C2["delta"] * F1
+    a = qg_inversion_matrix(g["wv2"], F1, F2)
+    filtr = spectral_filter(g["k"], g["l"], g["dx"], g["dy"], C2["filterfac"])
+    Qy = np.array([C2["beta"] + F1 * (C2["U1"] - C2["U2"]),
+                   C2["beta"] - F2 * (C2["U1"] - C2["U2"])])
+    Ubg = np.array([C2["U1"], C2["U2"]])
+    q0 = 1e-7 * np.random.default_rng(seed).standard_normal((2, nx, nx))
+    try:
+        import build_ref
+        if not build_ref.available():
+            build_ref.build(quiet=True)
+        mod = build_ref.load()
+        k = mod.PseudoSpectralKernel(2, nx, nx, threads, 0, 0)
+        k.ll = g["ll"]
+        k.kk = g["kk"]
+        k.a = a
+        k.Ubg = Ubg
+        k.Qy = Qy
+        k.filtr = filtr
+        k.rek = C2["rek"]
+        k.dt = dt
+        k.q = q0
+        step = lambda: (k._invert(), k._do_advection(), k._do_friction(), k._forward_timestep())
+        kind = "reference"
+    except Exception:
+        o = O.OracleKernel(2, nx, nx, a, g["kk"], g["ll"], Ubg, Qy, filtr, C2["rek"], dt)
+        o.set_q(q0)
+        step = o.step
+        kind = "port"
+        threads = 1
+    step()
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        step()
+    return time.perf_counter() - t0, kind, threads
+
+
+def cpu_baseline(dt, sample_steps):
+    secs, kind, cores = cpu_model_steps(sample_steps, dt=dt)
+    return {"value": sim_yr_per_hr(sample_steps, dt, secs), "unit": "sim-yr/hr",
+            "cores": cores, "kind": kind,
+            "sample": "%d config-2 steps (nx=256, FP64) on the host, %.1f ms/step"
+                      % (sample_steps, 1e3 * secs / sample_steps)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    dt = 3600.0
+    secs, kind, cores = cpu_model_steps(args.warmup)  # warm-up steps
+    times = []
+    for _ in range(args.steps):
+        s, kind, cores = cpu_model_steps(args.chunk, dt=dt)
+        times.append(s)
+    total = sum(times)
+    value = sim_yr_per_hr(args.steps * args.chunk, dt, total)
+    line = {"metric": METRIC, "value": value, "unit": "sim-yr/hr", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (config-2 physics), "
+                                   "%d model steps per timed step" % args.chunk,
+                       "model_steps_per_step": args.chunk, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": "sim-yr/hr", "cores": cores, "kind": kind,
+                             "sample": "%d x %d config-2 steps" % (args.steps, args.chunk)},
+            "e2e": {"value": value, "unit": "sim-yr/hr", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def algorithmic_bytes(nz, ny, nx):
+    """Compulsory HBM bytes of one FP64 model step with the state resident:
+    read qh, dqhdt_p, dqhdt_pp and write qh, dqhdt (16 B each per spectral
+    point) plus read and write q (8 B per grid point)."""
+    S = nz * ny * (nx // 2 + 1)
+    P = nz * ny * nx
+    return 80 * S + 16 * P
+
+
+def run_ours(args, rank, world, local_rank):
+    import ctypes
+    import torch
+    import pyqg_gb300 as P
+    from pyqg_gb300 import _lib
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    nx, dt = args.nx, 3600.0
+    m = P.QGModel(nx=nx, dt=dt, **C2, **QUIET)
+    q0 = 1e-7 * np.random.default_rng(1000 + rank).standard_normal((2, nx, nx))
+    m.q = q0
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    L = _lib.lib()
+
+    def state():
+        if m._role["dqhdt_p"] == m._role["dqhdt_pp"]:
+            m._own("dqhdt_pp", copy=True)
+        return _lib.State(m._ptr("q"), m._ptr("qh"), m._ptr("dqhdt"), m._ptr("dqhdt_p"),
+                          m._ptr("dqhdt_pp"), m._ablevel, m._tc, m._t, m._dt)
+
+    def commit(st):
+        idx = {b.data_ptr(): i for i, b in enumerate(m._tend)}
+        m._role = {"dqhdt": idx[st.dqhdt], "dqhdt_p": idx[st.dqhdt_p],
+                   "dqhdt_pp": idx[st.dqhdt_pp]}
+        m._ablevel, m._tc, m._t = st.ablevel, st.tc, st.t
+
+    def device_step():
+        st = state()
+        _lib.check(L.pqg_step(m._plan, ctypes.byref(st), args.chunk, None,
+                              ctypes.c_void_p(stream.cuda_stream)))
+        commit(st)
+
+    # warm-up (also captures and caches the CUDA graphs)
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clocks:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            device_step()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    model_steps = args.steps * args.chunk
+    value = world * sim_yr_per_hr(model_steps, dt, total_s)
+
+    # per-kernel durations (CUDA events around every launch, no graph)
+    st = state()
+    kms = (ctypes.c_double * 2)()
+    kcnt = (ctypes.c_int * 2)()
+    flush.zero_()
+    _lib.check(L.pqg_step_profile(m._plan, ctypes.byref(st), args.chunk, kms, kcnt,
+                                  ctypes.c_void_p(stream.cuda_stream)))
+    commit(st)
+    row_ms, col_ms = kms[0] / kcnt[0], kms[1] / kcnt[1]
+
+    # end to end through the public model API with host buffers
+    qhost = torch.from_numpy(q0.copy()).pin_memory().numpy()
+    for _ in range(2):
+        m.q = qhost
+        m.tmax = m.t + args.chunk * dt
+        m.run()
+        _ = m.q
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m.q = qhost                      # H2D of the step's input state
+        m.tmax = m.t + args.chunk * dt
+        m.run()
+        qout = m.q                       # D2H of the result
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = world * sim_yr_per_hr(model_steps, dt, e2e_s)
+    del qout
+
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    nz = 2
+    # dominant kernel: the larger of the two per-step kernels; its share of
+    # the step's compulsory bytes (column kernel: spectral state 80 S,
+    # row kernel: physical q 16 P)
+    S = nz * nx * (nx // 2 + 1)
+    Pn = nz * nx * nx
+    if col_ms >= row_ms:
+        name, kms_, nbytes = "k_col_fused", col_ms, 80 * S
+    else:
+        name, kms_, nbytes = "k_row_adv", row_ms, 16 * Pn
+    achieved = nbytes / (kms_ * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(HERE, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            with open(tf) as f:
+                traffic = json.load(f).get(name)
+        except Exception:
+            traffic = None
+    base = cpu_baseline(dt, args.cpu_sample)
+    line = {
+        "metric": METRIC, "value": value, "unit": "sim-yr/hr", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded 1e-7 N(0,1) initial PV)",
+        "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (config-2 physics), "
+                               "%d model steps per timed step" % args.chunk,
+                   "model_steps_per_step": args.chunk,
+                   "model_steps_per_s": model_steps * world / total_s,
+                   "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e, "unit": "sim-yr/hr", "h2d_bytes_per_step": int(q0.nbytes),
+                "d2h_bytes_per_step": int(q0.nbytes),
+                "api": "QGModel.q = host q; QGModel.run() for the chunk; QGModel.q"},
+        "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "kernel_ms": {"k_row_adv": row_ms, "k_col_fused": col_ms},
+                     "algorithmic_bytes_per_launch": nbytes,
+                     "note": "FP64 step: bound by the FP64 pipe, not HBM"},
+        "cpu_baseline": base,
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps * (2 * args.chunk + 2),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--chunk", type=int, default=100)
+    ap.add_argument("--nx", type=int, default=256)
+    ap.add_argument("--cpu-sample", type=int, default=1000)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/*
+ * pyqg_gb300 — C ABI of the GB300 (sm_103a) pseudo-spectral time step.
+ *
+ * The entry points replace, one for one, the hot-path interface of pyqg's
+ * Cython class `PseudoSpectralKernel` (pyqg/kernel.pyx:32-637): its
+ * constructor, its constant setters, its transforms and its five stage
+ * methods, plus a fused multi-step call that pyqg runs as a Python loop
+ * (`Model.run` -> `Model._step_forward`, pyqg/model.py:280-283,406-436).
+ *
+ * Conventions
+ *   - Shapes follow the reference: physical fields (nz, ny, nx) float64 and
+ *     spectral fields (nz, nl, nk) complex128 with nl = ny, nk = nx/2 + 1,
+ *     C order.  Complex arrays are interleaved (re, im) `double` pairs.
+ *   - Pointers to fields are DEVICE pointers (16-byte aligned); pointers to
+ *     constants (pqg_set_*) are HOST pointers, copied into the plan.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *     All compute calls are asynchronous on that stream.
+ *   - Every function returns PQG_OK (0) or a PQG_ERR_* code; the message of
+ *     the last error on the calling thread is returned by pqg_last_error().
+ *   - Transforms: pqg_rfft2 is unnormalised, pqg_irfft2 scales by 1/(nx ny)
+ *     and ignores the imaginary parts of the k = 0 and k = nx/2 columns after
+ *     the y transform, as numpy.fft.irfftn / FFTW c2r do.
+ */
+#ifndef PYQG_GB300_H
+#define PYQG_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PQG_OK 0
+#define PQG_ERR_INVALID 1      /* bad argument (NULL pointer, negative size) */
+#define PQG_ERR_UNSUPPORTED 2  /* grid size the kernels do not handle       */
+#define PQG_ERR_CUDA 3         /* CUDA runtime error (message has details)   */
+#define PQG_ERR_NOMEM 4        /* device or host allocation failed           */
+#define PQG_ERR_STATE 5        /* call out of order (e.g. constants unset)   */
+
+typedef struct pqg_plan pqg_plan;
+
+/* Optional outputs of the last step of pqg_step (any may be NULL). These are
+ * the intermediates the reference keeps as state after `_step_forward`:
+ * ph, uh, vh (spectral) and u, v, uq, vq (physical), uqh, vqh (spectral). */
+typedef struct pqg_aux {
+    double *ph, *uh, *vh;
+    double *u, *v, *uq, *vq;
+    double *uqh, *vqh;
+} pqg_aux;
+
+/* Time-stepping state for pqg_step.  `dqhdt_p` and `dqhdt_pp` must be
+ * distinct buffers.  pqg_step rotates the history pointers the way the
+ * reference rotates the values (pyqg/kernel.pyx:509-510): on return
+ * `dqhdt` and `dqhdt_p` point to the same buffer (the newest tendency). */
+typedef struct pqg_state {
+    double *q;          /* (nz, ny, nx) physical PV                    */
+    double *qh;         /* (nz, nl, nk) spectral PV                    */
+    double *dqhdt;      /* newest tendency (output only)               */
+    double *dqhdt_p;    /* previous tendency                           */
+    double *dqhdt_pp;   /* tendency before previous (overwritten)      */
+    int ablevel;        /* 0: forward Euler next, 1: AB2, >=2: AB3     */
+    long long tc;       /* step counter  (pyqg/kernel.pyx:98)          */
+    double t;           /* model time    (pyqg/kernel.pyx:99)          */
+    double dt;          /* time step     (pyqg/kernel.pyx:97)          */
+} pqg_state;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int pqg_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *pqg_last_error(void);
+
+/* Create / destroy a plan for an (nz, ny, nx) grid: FFT descriptors,
+ * twiddle tables, constants and the transposition scratch (device memory).
+ * Replaces PseudoSpectralKernel.__init__ (pyqg/kernel.pyx:120-206).
+ * nx and ny must be even; nx/2 and ny must factor into 2, 3 and 5 and be
+ * at most 2048; 3*nz*ny*16 bytes must fit the per-block shared memory. */
+int pqg_plan_create(pqg_plan **plan, int nz, int ny, int nx);
+int pqg_plan_destroy(pqg_plan *plan);
+
+/* Constants (host arrays, copied).  Setting the wavenumbers also sets
+ * k2l2 = kk^2 + ll^2 and the ikQy table.
+ *   kk (nk), ll (nl)          -> pyqg/kernel.pyx:536-556 (kk, ll setters)
+ *   k2l2 (nl, nk)             -> pyqg/kernel.pyx:82 (public _k2l2)
+ *   a (nz, nz, nl, nk) real   -> pyqg/kernel.pyx:557-563 (a setter)
+ *   Ubg (nz)                  -> pyqg/kernel.pyx:564-568 (Ubg setter)
+ *   Qy (nz)                   -> pyqg/kernel.pyx:569-575 (Qy setter, ikQy)
+ *   filtr (nl, nk)            -> pyqg/kernel.pyx:90 (public filtr)
+ *   rek                       -> pyqg/kernel.pyx:93 (public rek)         */
+int pqg_set_wavenumbers(pqg_plan *plan, const double *kk, const double *ll);
+int pqg_set_k2l2(pqg_plan *plan, const double *k2l2);
+int pqg_set_inversion(pqg_plan *plan, const double *a);
+int pqg_set_ubg(pqg_plan *plan, const double *Ubg);
+int pqg_set_qy(pqg_plan *plan, const double *Qy);
+int pqg_set_filter(pqg_plan *plan, const double *filtr);
+int pqg_set_rek(pqg_plan *plan, double rek);
+
+/* Batched 2-D real transforms over `nplanes` (ny, nx) planes.
+ * Replace the planned transforms and the fft/ifft helpers
+ * (pyqg/kernel.pyx:208-267,291-309). */
+int pqg_rfft2(pqg_plan *plan, const double *x, double *xh, int nplanes,
+              void *stream);
+int pqg_irfft2(pqg_plan *plan, const double *xh, double *x, int nplanes,
+               void *stream);
+
+/* _invert (pyqg/kernel.pyx:312-355): ph = a qh, uh = -il ph, vh = ik ph,
+ * u = irfft2(uh), v = irfft2(vh).  ph/uh/vh may be NULL (not stored). */
+int pqg_invert(pqg_plan *plan, const double *qh, double *ph, double *uh,
+               double *vh, double *u, double *v, void *stream);
+
+/* _do_advection (pyqg/kernel.pyx:357-395): uq = (u + Ubg) q, vq = v q,
+ * uqh, vqh = rfft2, dqhdt = -(ik uqh + il vqh + ikQy ph).  uq, vq, uqh and
+ * vqh may be NULL (not stored). */
+int pqg_do_advection(pqg_plan *plan, const double *q, const double *u,
+                     const double *v, const double *ph, double *uq,
+                     double *vq, double *uqh, double *vqh, double *dqhdt,
+                     void *stream);
+
+/* _do_friction (pyqg/kernel.pyx:444-461): if rek != 0,
+ * dqhdt[nz-1] += rek k2l2 ph[nz-1]. */
+int pqg_do_friction(pqg_plan *plan, const double *ph, double *dqhdt,
+                    void *stream);
+
+/* Spectral part of _do_q_subgrid_parameterization (pyqg/kernel.pyx:424-442):
+ * dqh = rfft2(dq); dqhdt += dqh.  dqh may be NULL. */
+int pqg_do_q_forcing(pqg_plan *plan, const double *dq, double *dqh,
+                     double *dqhdt, void *stream);
+
+/* Spectral part of _do_uv_subgrid_parameterization
+ * (pyqg/kernel.pyx:397-422): duh, dvh = rfft2(du, dv);
+ * dqhdt += -il duh + ik dvh.  duh and dvh may be NULL. */
+int pqg_do_uv_forcing(pqg_plan *plan, const double *du, const double *dv,
+                      double *duh, double *dvh, double *dqhdt, void *stream);
+
+/* _forward_timestep (pyqg/kernel.pyx:463-526): FE/AB2/AB3 by `ablevel`,
+ * qh = filtr (qh + dt1 dqhdt + dt2 dqhdt_p + dt3 dqhdt_pp), q = irfft2(qh).
+ * With rotate != 0 the history is also shifted in place
+ * (dqhdt_pp <- dqhdt_p, dqhdt_p <- dqhdt) exactly as the reference does;
+ * with rotate == 0 the caller rotates its buffer roles instead. */
+int pqg_forward_timestep(pqg_plan *plan, int ablevel, double dt, double *qh,
+                         const double *dqhdt, double *dqhdt_p,
+                         double *dqhdt_pp, double *q, int rotate,
+                         void *stream);
+
+/* `nsteps` whole steps without parameterization hooks, in the order of
+ * pyqg/model.py:406-436 (_invert, _do_advection, _do_friction,
+ * _forward_timestep), fused into two kernels per step and replayed from a
+ * cached CUDA graph.  Updates *state (q, qh, history pointers, ablevel, tc,
+ * t).  `aux` (may be NULL) receives the intermediates of the last step. */
+int pqg_step(pqg_plan *plan, pqg_state *state, int nsteps,
+             const pqg_aux *aux, void *stream);
+
+/* Instrumentation for the profile / bench tooling (no counterpart in the
+ * reference): `nsteps` fused steps like pqg_step but launched one by one
+ * (no graph) with CUDA events around each kernel.  On return ms[0] / ms[1]
+ * hold the summed durations of the row / column kernels and counts[0] /
+ * counts[1] their launch counts.  Synchronizes `stream`. */
+int pqg_step_profile(pqg_plan *plan, pqg_state *state, int nsteps,
+                     double *ms, int *counts, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYQG_GB300_H */

@@ -1,0 +1,120 @@
+"""Build recipe for the reference pseudo-spectral kernel (test infrastructure).
+
+This script is part of the oracle: it is used only by the tests, by
+``__graft_entry__.smoke()`` and by ``bench.py``'s CPU-baseline leg, never by
+the product path.
+
+It compiles the reference's own hot path, ``pyqg/kernel.pyx`` (the Cython
+``PseudoSpectralKernel``), from the file where it lies in the reference tree,
+with the reference's numpy.fft fallback selected (``PYQG_USE_PYFFTW = 0``,
+``pyqg/kernel.pyx:13-19,245-267``; pyFFTW/FFTW are not available here).  All
+outputs go to ``oracle/_ref/`` which is git-ignored.
+
+Two stages, so that the result can also be built on a machine without the
+reference tree or Cython:
+
+``cythonize``  needs the reference tree and Cython.  Writes
+               ``oracle/_ref/pyqg_ref_kernel.c`` (generated C).
+``compile``    needs gcc, the Python headers and numpy.  Compiles that C file
+               with ``-O3 -fopenmp`` (``setup.py:77-124`` of the reference uses
+               ``-fopenmp`` the same way) into ``oracle/_ref/pyqg_ref_kernel*.so``.
+
+Usage: ``python oracle/build_ref.py [cythonize] [compile]`` (both by default).
+"""
+import os
+import shutil
+import subprocess
+import sys
+import sysconfig
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+REF_ROOT = os.environ.get("PYQG_REFERENCE_ROOT", "/root/reference")
+REF_KERNEL = os.path.join(REF_ROOT, "pyqg", "kernel.pyx")
+MODNAME = "pyqg_ref_kernel"
+C_FILE = os.path.join(OUT, MODNAME + ".c")
+
+
+def so_path():
+    suffix = sysconfig.get_config_var("EXT_SUFFIX") or ".so"
+    return os.path.join(OUT, MODNAME + suffix)
+
+
+def cythonize():
+    """Generate C from the reference kernel.pyx (numpy.fft fallback)."""
+    if not os.path.exists(REF_KERNEL):
+        raise FileNotFoundError(REF_KERNEL)
+    os.makedirs(OUT, exist_ok=True)
+    inc = os.path.join(OUT, "include")
+    os.makedirs(inc, exist_ok=True)
+    # setup.py:67-75 of the reference generates this file at build time.
+    with open(os.path.join(inc, ".compile_time_use_pyfftw.pxi"), "w") as f:
+        f.write("DEF PYQG_USE_PYFFTW = 0\n")
+    cmd = [sys.executable, "-m", "cython", "-3", "--module-name", MODNAME,
+           "-I", inc, "-o", C_FILE, REF_KERNEL]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.PIPE)
+    return C_FILE
+
+
+def compile_c():
+    """Compile the generated C into an importable extension module."""
+    import numpy as np
+    if not os.path.exists(C_FILE):
+        raise FileNotFoundError(C_FILE)
+    pyinc = sysconfig.get_paths()["include"]
+    if not os.path.exists(os.path.join(pyinc, "Python.h")):
+        raise RuntimeError("Python.h not found in " + pyinc)
+    out = so_path()
+    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared",
+           "-DNPY_NO_DEPRECATED_API=NPY_1_7_API_VERSION",
+           "-I", pyinc, "-I", np.get_include(), C_FILE, "-o", out]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.PIPE)
+    return out
+
+
+def available():
+    return os.path.exists(so_path())
+
+
+def load():
+    """Import the compiled reference kernel module (or raise ImportError)."""
+    import importlib.util
+    path = so_path()
+    if not os.path.exists(path):
+        raise ImportError("reference kernel not built: " + path)
+    spec = importlib.util.spec_from_file_location(MODNAME, path)
+    mod = importlib.util.module_from_spec(spec)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        spec.loader.exec_module(mod)
+    return mod
+
+
+def build(quiet=True):
+    """Cythonize when the reference tree is present, then compile.
+
+    Returns the path of the built module or None when it cannot be built.
+    """
+    try:
+        if os.path.exists(REF_KERNEL):
+            cythonize()
+        if os.path.exists(C_FILE):
+            return compile_c()
+    except (subprocess.CalledProcessError, RuntimeError, OSError) as e:
+        if not quiet:
+            raise
+        msg = getattr(e, "stderr", b"") or b""
+        print("oracle/_ref build skipped:", e, msg.decode()[-400:],
+              file=sys.stderr)
+    return None
+
+
+if __name__ == "__main__":
+    stages = sys.argv[1:] or ["cythonize", "compile"]
+    if "cythonize" in stages:
+        print(cythonize())
+    if "compile" in stages:
+        print(compile_c())

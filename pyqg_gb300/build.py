@@ -1,0 +1,60 @@
+"""Build the CUDA library ``libpyqg_gb300.so`` in-tree for sm_103a.
+
+``python -m pyqg_gb300.build`` (or ``__graft_entry__.build()``) compiles
+``csrc/*.cu`` with nvcc into ``pyqg_gb300/lib/``.  Host code is compiled with
+``-ffp-contract=off`` so host-side constant tables round identically on
+x86-64 and aarch64.
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "lib")
+LIBNAME = "libpyqg_gb300.so"
+ARCH = os.environ.get("PQG_CUDA_ARCH", "103a")
+
+
+def nvcc_path():
+    cand = os.environ.get("NVCC") or shutil.which("nvcc")
+    if cand:
+        return cand
+    default = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(default):
+        return default
+    raise RuntimeError("nvcc not found")
+
+
+def sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                  if f.endswith(".cu"))
+
+
+def lib_path():
+    return os.path.join(LIBDIR, LIBNAME)
+
+
+def build(verbose=False, extra_flags=()):
+    """Compile the library; returns its path."""
+    os.makedirs(LIBDIR, exist_ok=True)
+    out = lib_path()
+    tmp = out + ".tmp"
+    cmd = [nvcc_path(), "-O3", "-std=c++17", "-shared", "-lineinfo",
+           "-gencode", "arch=compute_%s,code=sm_%s" % (ARCH, ARCH),
+           "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
+           "-Xptxas", "-O3",
+           "-I", os.path.join(os.path.dirname(HERE), "include"),
+           *extra_flags, *sources(), "-o", tmp]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if verbose or res.returncode != 0:
+        sys.stderr.write(res.stdout + res.stderr)
+    if res.returncode != 0:
+        raise RuntimeError("nvcc failed (exit %d)" % res.returncode)
+    os.replace(tmp, out)
+    return out
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,1128 @@
+// GB300 (sm_103a) FP64 pseudo-spectral time step of pyqg, behind a C ABI.
+//
+// Data layout in device memory (C order, complex = interleaved double2):
+//   physical  (nz, ny, nx) double          q, u, v, uq, vq
+//   spectral  (nz, nl, nk) double2         qh, ph, uh, vh, uqh, vqh, dqhdt*
+//   mixed     (plane, ny, nk) double2      plan-owned scratch between the row
+//             pass (x transforms) and the column pass (y transforms)
+//
+// A 2-D real transform is split into a row pass (length-nx real FFT of every
+// row, done as a length-nx/2 complex FFT plus packing) and a column pass
+// (length-ny complex FFT of every column k).  The row pass runs first on the
+// forward transform, the column pass first on the inverse, matching
+// numpy.fft.rfftn / irfftn axis order.  A whole time step is two kernels:
+//   row kernel    C2R of (u, v, q) -> products (u+Ubg)q, vq -> R2C
+//   column kernel FFT_y of (uq, vq) -> tendency, drag, filtered AB3 update ->
+//                 inversion of the new qh -> IFFT_y of (uh, vh, qh)
+// The column kernel runs one CTA per (layer, column); the nz CTAs of a
+// column form a thread-block cluster and exchange the per-layer qh values
+// the layer coupling needs through distributed shared memory.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pyqg_gb300.h"
+#include "pqg_fft.cuh"
+
+namespace cg = cooperative_groups;
+using namespace pqg;
+
+// ===========================================================================
+// error reporting
+// ===========================================================================
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define PQG_CUDA(call)                                                    \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess)                                                \
+      return fail(PQG_ERR_CUDA, std::string(#call) + ": " +               \
+                                    cudaGetErrorString(e_));              \
+  } while (0)
+
+// ===========================================================================
+// kernel argument blocks
+// ===========================================================================
+struct Geo {
+  int nz, ny, nx, nk, M;  // M = nx / 2
+  double scale;           // 1 / (nx * ny)
+  FftDesc fx;             // complex length M
+  FftDesc fy;             // complex length ny
+  const double2* twx;     // nx entries exp(-2 pi i m / nx)
+  const double2* twy;     // ny entries exp(-2 pi i m / ny)
+};
+
+struct Consts {
+  const double* a;      // (nz, nz, nl, nk)
+  const double* kk;     // (nk)
+  const double* ll;     // (nl)
+  const double* k2l2;   // (nl, nk)
+  const double* kQy;    // (nz, nk)   kk * Qy
+  const double* Ubg;    // (nz)
+  const double* filtr;  // (nl, nk)
+  double rek;
+};
+
+// load a twiddle table into shared memory
+__device__ __forceinline__ void load_tw(double2* s, const double2* __restrict__ g, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = g[i];
+}
+
+// ===========================================================================
+// ROW PASS
+// ===========================================================================
+// Row kernel: one CTA handles `rb` consecutive rows r = z*ny + y of all
+// fields it touches.  Shared layout: [tw_x (nx)] [field][row][M].
+//
+// mode ROW_ADV  (advection, reference _do_advection first half, fused step):
+//   U, V from mixed (C2R) or physical; Q from mixed (C2R) or physical;
+//   optional stores of u, v, q, uq, vq; R2C of uq, vq -> mixed UQ, VQ.
+// mode ROW_C2R  (nf fields mixed -> physical)
+// mode ROW_R2C  (nf fields physical -> mixed)
+struct RowAdvArgs {
+  const double2* mixU; const double2* mixV; const double2* mixQ;
+  const double* physU; const double* physV; const double* physQ;
+  double* outU; double* outV; double* outQ; double* outUQ; double* outVQ;
+  double2* mixUQ; double2* mixVQ;
+  const double* Ubg;
+  int rb;
+};
+
+__global__ void k_row_adv(Geo g, RowAdvArgs A) {
+  extern __shared__ double2 sm[];
+  const int M = g.M, nk = g.nk, nx = g.nx;
+  const int nrows = g.nz * g.ny;
+  const int r0 = blockIdx.x * A.rb;
+  const int rb = min(A.rb, nrows - r0);
+  double2* tw = sm;
+  double2* bU = sm + nx;
+  double2* bV = bU + A.rb * M;
+  double2* bQ = bV + A.rb * M;
+  load_tw(tw, g.twx, nx);
+  __syncthreads();
+
+  // -- load / C2R pre-processing --------------------------------------------
+  const int half = M / 2 + 1;
+  for (int t = threadIdx.x; t < 3 * rb * half; t += blockDim.x) {
+    const int f = t / (rb * half);
+    const int rem = t - f * rb * half;
+    const int rr = rem / half, k = rem - rr * half;
+    const int r = r0 + rr;
+    const double2* mix = f == 0 ? A.mixU : (f == 1 ? A.mixV : A.mixQ);
+    const double* phys = f == 0 ? A.physU : (f == 1 ? A.physV : A.physQ);
+    double2* b = (f == 0 ? bU : (f == 1 ? bV : bQ)) + rr * M;
+    if (mix) {
+      c2r_pre(mix + (size_t)r * nk, b, M, k, tw);
+    } else {
+      const double2* row = reinterpret_cast<const double2*>(phys + (size_t)r * nx);
+      // k-th task copies complex slots k and M-1-k
+      if (k < M - k) b[k] = row[k];
+      if (k < M - k && M - 1 - k != k) b[M - 1 - k] = row[M - 1 - k];
+    }
+  }
+  __syncthreads();
+
+  // -- inverse transforms of the mixed inputs (U, V[, Q] are a prefix) -------
+  // Buffers of a field hold A.rb rows; rows past `rb` (last CTA) are unused.
+  {
+    const int nmix = (A.mixU ? 1 : 0) + (A.mixV ? 1 : 0) + (A.mixQ ? 1 : 0);
+    if (nmix) fft_run<true>(bU, M, nmix * A.rb, g.fx, tw, 2);
+  }
+
+  // -- unpack, products, optional stores -------------------------------------
+  const double s = g.scale;
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    const int r = r0 + rr;
+    const int z = r / g.ny;
+    double2 u = bU[rr * M + m], v = bV[rr * M + m], q = bQ[rr * M + m];
+    if (A.mixU) u = cscale(u, s);
+    if (A.mixV) v = cscale(v, s);
+    if (A.mixQ) q = cscale(q, s);
+    const size_t po = (size_t)r * nx + 2 * m;
+    if (A.outU) *reinterpret_cast<double2*>(A.outU + po) = u;
+    if (A.outV) *reinterpret_cast<double2*>(A.outV + po) = v;
+    if (A.outQ) *reinterpret_cast<double2*>(A.outQ + po) = q;
+    // uq = (u + Ubg) q, vq = v q (pyqg/kernel.pyx:377-378)
+    const double ub = A.Ubg[z];
+    const double2 uq = make_double2(__dmul_rn(__dadd_rn(u.x, ub), q.x),
+                                    __dmul_rn(__dadd_rn(u.y, ub), q.y));
+    const double2 vq = make_double2(__dmul_rn(v.x, q.x), __dmul_rn(v.y, q.y));
+    if (A.outUQ) *reinterpret_cast<double2*>(A.outUQ + po) = uq;
+    if (A.outVQ) *reinterpret_cast<double2*>(A.outVQ + po) = vq;
+    bU[rr * M + m] = uq;
+    bV[rr * M + m] = vq;
+  }
+  __syncthreads();
+
+  // -- forward transforms of uq, vq and R2C post-processing -------------------
+  fft_run<false>(bU, M, 2 * A.rb, g.fx, tw, 2);
+  for (int t = threadIdx.x; t < 2 * rb * half; t += blockDim.x) {
+    const int f = t / (rb * half);
+    const int rem = t - f * rb * half;
+    const int rr = rem / half, k = rem - rr * half;
+    const int r = r0 + rr;
+    double2* X = (f == 0 ? A.mixUQ : A.mixVQ) + (size_t)r * nk;
+    r2c_post((f == 0 ? bU : bV) + rr * M, X, M, k, tw);
+  }
+}
+
+// nf planes-of-fields: mixed -> physical (second half of irfft2)
+struct RowBatchArgs {
+  const double2* mix; double* phys;   // plane-major, nplanes planes
+  const double2* mixsrc; const double* physsrc;
+  double2* mixdst;
+  int nrows;                          // nplanes * ny
+  int rb;
+};
+
+__global__ void k_row_c2r(Geo g, RowBatchArgs A) {
+  extern __shared__ double2 sm[];
+  const int M = g.M, nk = g.nk, nx = g.nx;
+  const int r0 = blockIdx.x * A.rb;
+  const int rb = min(A.rb, A.nrows - r0);
+  double2* tw = sm;
+  double2* b = sm + nx;
+  load_tw(tw, g.twx, nx);
+  __syncthreads();
+  const int half = M / 2 + 1;
+  for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
+    const int rr = t / half, k = t - rr * half;
+    c2r_pre(A.mixsrc + (size_t)(r0 + rr) * nk, b + rr * M, M, k, tw);
+  }
+  __syncthreads();
+  fft_run<true>(b, M, rb, g.fx, tw, 2);
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    const double2 x = cscale(b[rr * M + m], g.scale);
+    *reinterpret_cast<double2*>(A.phys + (size_t)(r0 + rr) * nx + 2 * m) = x;
+  }
+}
+
+__global__ void k_row_r2c(Geo g, RowBatchArgs A) {
+  extern __shared__ double2 sm[];
+  const int M = g.M, nk = g.nk, nx = g.nx;
+  const int r0 = blockIdx.x * A.rb;
+  const int rb = min(A.rb, A.nrows - r0);
+  double2* tw = sm;
+  double2* b = sm + nx;
+  load_tw(tw, g.twx, nx);
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    b[rr * M + m] = reinterpret_cast<const double2*>(A.physsrc + (size_t)(r0 + rr) * nx)[m];
+  }
+  __syncthreads();
+  fft_run<false>(b, M, rb, g.fx, tw, 2);
+  const int half = M / 2 + 1;
+  for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
+    const int rr = t / half, k = t - rr * half;
+    r2c_post(b + rr * M, A.mixdst + (size_t)(r0 + rr) * nk, M, k, tw);
+  }
+}
+
+// ===========================================================================
+// COLUMN PASS
+// ===========================================================================
+// One CTA per (plane or layer z = blockIdx.x, column k = blockIdx.y).
+// Shared layout: [tw_y (ny)] [sequence][ny].
+
+// column of a (plane, ny, nk) array
+__device__ __forceinline__ size_t cidx(int plane, int l, int k, int ny, int nk) {
+  return ((size_t)plane * ny + l) * nk + k;
+}
+
+// generic column FFT over planes: spectral <- mixed (forward, rfft2 2nd half)
+// or mixed <- spectral (inverse, irfft2 1st half)
+template <bool INV>
+__global__ void k_col_batch(Geo g, const double2* __restrict__ src,
+                            double2* __restrict__ dst) {
+  extern __shared__ double2 sm[];
+  const int ny = g.ny, nk = g.nk;
+  const int p = blockIdx.x, k = blockIdx.y;
+  double2* tw = sm;
+  double2* b = sm + ny;
+  load_tw(tw, g.twy, ny);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) b[l] = src[cidx(p, l, k, ny, nk)];
+  __syncthreads();
+  fft_run<INV>(b, ny, 1, g.fy, tw, 1);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) dst[cidx(p, l, k, ny, nk)] = b[l];
+}
+
+// _invert, column part: ph = a qh; uh = -il ph; vh = ik ph (optionally
+// stored); inverse y transforms of uh, vh -> mixed U, V.
+__global__ void k_col_invert(Geo g, Consts c, const double2* __restrict__ qh,
+                             double2* ph, double2* uh, double2* vh,
+                             double2* mixU, double2* mixV) {
+  extern __shared__ double2 sm[];
+  const int ny = g.ny, nk = g.nk, nz = g.nz;
+  const int z = blockIdx.x, k = blockIdx.y;
+  double2* tw = sm;
+  double2* bU = sm + ny;
+  double2* bV = bU + ny;
+  load_tw(tw, g.twy, ny);
+  const double kk = c.kk[k];
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    double2 p = make_double2(0.0, 0.0);
+    for (int z1 = 0; z1 < nz; z1++)
+      p = ph_acc(p, c.a[cidx(z * nz + z1, l, k, ny, nk)], qh[cidx(z1, l, k, ny, nk)]);
+    const double2 u = uh_of(c.ll[l], p), v = vh_of(kk, p);
+    const size_t o = cidx(z, l, k, ny, nk);
+    if (ph) ph[o] = p;
+    if (uh) uh[o] = u;
+    if (vh) vh[o] = v;
+    bU[l] = u;
+    bV[l] = v;
+  }
+  __syncthreads();
+  fft_run<true>(bU, ny, 2, g.fy, tw, 1);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    mixU[cidx(z, l, k, ny, nk)] = bU[l];
+    mixV[cidx(z, l, k, ny, nk)] = bV[l];
+  }
+}
+
+// _do_advection, column part: y transforms of mixed UQ, VQ -> uqh, vqh
+// (optionally stored); dqhdt = -(ik uqh + il vqh + ikQy ph).
+__global__ void k_col_adv(Geo g, Consts c, const double2* __restrict__ mixUQ,
+                          const double2* __restrict__ mixVQ,
+                          const double2* __restrict__ ph, double2* uqh,
+                          double2* vqh, double2* dqhdt) {
+  extern __shared__ double2 sm[];
+  const int ny = g.ny, nk = g.nk;
+  const int z = blockIdx.x, k = blockIdx.y;
+  double2* tw = sm;
+  double2* bU = sm + ny;
+  double2* bV = bU + ny;
+  load_tw(tw, g.twy, ny);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    bU[l] = mixUQ[cidx(z, l, k, ny, nk)];
+    bV[l] = mixVQ[cidx(z, l, k, ny, nk)];
+  }
+  __syncthreads();
+  fft_run<false>(bU, ny, 2, g.fy, tw, 1);
+  const double kk = c.kk[k], kQy = c.kQy[z * nk + k];
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    const double2 a = bU[l], b = bV[l];
+    if (uqh) uqh[o] = a;
+    if (vqh) vqh[o] = b;
+    dqhdt[o] = tendency(kk, c.ll[l], kQy, a, b, ph[o]);
+  }
+}
+
+// _forward_timestep, column part: filtered AB update of qh (stored), optional
+// in-place history shift, inverse y transform of the new qh -> mixed Q.
+__global__ void k_col_ab3(Geo g, Consts c, double2* qh,
+                          const double2* __restrict__ dq, double2* dqp,
+                          double2* dqpp, double c1, double c2, double c3,
+                          int rotate, double2* mixQ) {
+  extern __shared__ double2 sm[];
+  const int ny = g.ny, nk = g.nk;
+  const int z = blockIdx.x, k = blockIdx.y;
+  double2* tw = sm;
+  double2* b = sm + ny;
+  load_tw(tw, g.twy, ny);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    const double2 d = dq[o], p = dqp[o], pp = dqpp[o];
+    const double2 qn = ab_update(c.filtr[(size_t)l * nk + k], qh[o], d, p, pp, c1, c2, c3);
+    qh[o] = qn;
+    if (rotate) {
+      dqpp[o] = p;
+      dqp[o] = d;
+    }
+    b[l] = qn;
+  }
+  __syncthreads();
+  fft_run<true>(b, ny, 1, g.fy, tw, 1);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) mixQ[cidx(z, l, k, ny, nk)] = b[l];
+}
+
+// _do_friction (pyqg/kernel.pyx:447-461), bottom layer only
+__global__ void k_friction(Geo g, Consts c, const double2* __restrict__ ph, double2* dqhdt) {
+  const int n = g.ny * g.nk;
+  const size_t off = (size_t)(g.nz - 1) * n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double rk2 = __dmul_rn(c.rek, c.k2l2[i]);
+    dqhdt[off + i] = friction(dqhdt[off + i], rk2, ph[off + i]);
+  }
+}
+
+// dqhdt += dqh (pyqg/kernel.pyx:436-441)
+__global__ void k_add_q(Geo g, const double2* __restrict__ dqh, double2* dqhdt) {
+  const size_t n = (size_t)g.nz * g.ny * g.nk;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double2 a = dqhdt[i], b = dqh[i];
+    dqhdt[i] = cadd(a, b);
+  }
+}
+
+// dqhdt += -il duh + ik dvh (pyqg/kernel.pyx:412-421)
+__global__ void k_add_uv(Geo g, Consts c, const double2* __restrict__ duh,
+                         const double2* __restrict__ dvh, double2* dqhdt) {
+  const size_t n = (size_t)g.nz * g.ny * g.nk;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % g.nk);
+    const int l = (int)((i / g.nk) % g.ny);
+    dqhdt[i] = uv_curl_add(dqhdt[i], c.kk[k], c.ll[l], duh[i], dvh[i]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused column kernel of one time step.  Grid (nz, nk), cluster (nz, 1, 1):
+// the CTA of layer z = cluster rank z handles column k of that layer.
+//   1. load mixed UQ, VQ and the current qh of this layer; FFT_y of UQ, VQ
+//   2. ph = sum a qh (qh of other layers read from their CTAs' shared memory)
+//      tendency + drag (+ optional spectral forcing), filtered AB update
+//   3. ph_new = sum a qh_new (other layers via shared memory), uh, vh
+//   4. IFFT_y of uh, vh, qh_new -> mixed U, V, Q for the next step
+// Mixed UQ/VQ alias mixed U/V: a CTA reads its column before writing it and
+// no other CTA touches that column.
+struct FusedColArgs {
+  double2* qh;                 // in: current, out: new
+  const double2* dqp;          // previous tendency
+  double2* dqpp;               // tendency before previous (read)
+  double2* dqout;              // new tendency (may equal dqpp)
+  const double2* forcing;      // optional spectral forcing added to dqhdt
+  double2* mixUQ; double2* mixVQ;   // in
+  double2* mixU; double2* mixV; double2* mixQ;  // out
+  double2* ph; double2* uh; double2* vh; double2* uqh; double2* vqh;  // aux
+  double c1, c2, c3;
+};
+
+__global__ void k_col_fused(Geo g, Consts c, FusedColArgs A) {
+  extern __shared__ double2 sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int ny = g.ny, nk = g.nk, nz = g.nz;
+  const int z = blockIdx.x, k = blockIdx.y;
+  double2* tw = sm;
+  double2* bU = sm + ny;      // UQ, later U
+  double2* bV = bU + ny;      // VQ, later V
+  double2* bQN = bV + ny;     // qh (new) of this layer
+  double2* bQO = bQN + ny;    // qh (old) of this layer
+  load_tw(tw, g.twy, ny);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    bU[l] = A.mixUQ[o];
+    bV[l] = A.mixVQ[o];
+    bQO[l] = A.qh[o];
+  }
+  __syncthreads();
+  fft_run<false>(bU, ny, 2, g.fy, tw, 1);
+  cluster.sync();  // qh(old) of every layer is in shared memory
+
+  const double kk = c.kk[k], kQy = c.kQy[z * nk + k];
+  const bool drag = (c.rek != 0.0) && (z == nz - 1);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    double2 p = make_double2(0.0, 0.0);
+    for (int z1 = 0; z1 < nz; z1++) {
+      const double2* rq = cluster.map_shared_rank(bQO, z1);
+      p = ph_acc(p, c.a[cidx(z * nz + z1, l, k, ny, nk)], rq[l]);
+    }
+    const double2 uqh = bU[l], vqh = bV[l];
+    const double ll = c.ll[l];
+    if (A.ph) A.ph[o] = p;
+    if (A.uh) A.uh[o] = uh_of(ll, p);
+    if (A.vh) A.vh[o] = vh_of(kk, p);
+    if (A.uqh) A.uqh[o] = uqh;
+    if (A.vqh) A.vqh[o] = vqh;
+    double2 d = tendency(kk, ll, kQy, uqh, vqh, p);
+    if (drag) d = friction(d, __dmul_rn(c.rek, c.k2l2[(size_t)l * nk + k]), p);
+    if (A.forcing) d = cadd(d, A.forcing[o]);
+    const double2 pv = A.dqp[o], ppv = A.dqpp[o];
+    const double2 qn = ab_update(c.filtr[(size_t)l * nk + k], bQO[l], d, pv, ppv, A.c1, A.c2, A.c3);
+    A.qh[o] = qn;
+    A.dqout[o] = d;
+    bQN[l] = qn;
+  }
+  cluster.sync();  // qh(new) of every layer is in shared memory
+
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    double2 p = make_double2(0.0, 0.0);
+    for (int z1 = 0; z1 < nz; z1++) {
+      const double2* rq = cluster.map_shared_rank(bQN, z1);
+      p = ph_acc(p, c.a[cidx(z * nz + z1, l, k, ny, nk)], rq[l]);
+    }
+    bU[l] = uh_of(c.ll[l], p);
+    bV[l] = vh_of(kk, p);
+  }
+  cluster.sync();  // remote reads of bQN done before it is transformed
+  fft_run<true>(bU, ny, 3, g.fy, tw, 1);  // U, V, qh(new): contiguous
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    A.mixU[o] = bU[l];
+    A.mixV[o] = bV[l];
+    A.mixQ[o] = bQN[l];
+  }
+}
+
+// ===========================================================================
+// plan
+// ===========================================================================
+struct GraphEntry {
+  std::vector<const void*> key;
+  double c[3];
+  int nsteps;
+  cudaGraphExec_t exec;
+};
+
+struct pqg_plan {
+  int nz, ny, nx, nk, M;
+  FftDesc fx, fy;
+  double2* twx = nullptr;
+  double2* twy = nullptr;
+  double* a = nullptr;
+  double* kk = nullptr;
+  double* ll = nullptr;
+  double* k2l2 = nullptr;
+  double* kQy = nullptr;
+  double* Ubg = nullptr;
+  double* filtr = nullptr;
+  double rek = 0.0;
+  std::vector<double> h_kk, h_ll, h_Qy;
+  bool have_kk = false, have_ll = false, have_qy = false;
+  double2* scratch = nullptr;  // mixed planes
+  int scratch_planes = 0;
+  int T_row = 128, rb = 1, T_col = 256;
+  int T_row_batch = 128, rb_batch = 1;
+  cudaStream_t cap_stream = nullptr;
+  std::vector<GraphEntry> graphs;
+  bool use_graphs = true;
+};
+
+static bool factor(int n, FftDesc& d) {
+  d.n = n;
+  d.nst = 0;
+  d.code = 0;
+  int m = n;
+  auto push = [&](int r) { d.code |= (unsigned long long)r << (4 * d.nst); d.nst++; m /= r; };
+  // radix-4 first, then 2, 3, 5 (radix order only affects rounding)
+  while (m % 4 == 0 && d.nst < kMaxStages) push(4);
+  while (m % 2 == 0 && d.nst < kMaxStages) push(2);
+  while (m % 3 == 0 && d.nst < kMaxStages) push(3);
+  while (m % 5 == 0 && d.nst < kMaxStages) push(5);
+  return m == 1;
+}
+
+// Smallest block size for which every Stockham stage of `d` fits:
+// blockDim * MaxIt<R> >= n / R.
+static int min_threads(const FftDesc& d) {
+  int t = 1;
+  for (int s = 0; s < d.nst; s++) {
+    const int r = d.radix(s);
+    const int it = r == 2 ? MaxIt<2>::value : r == 3 ? MaxIt<3>::value : r == 4 ? MaxIt<4>::value
+                 : r == 5 ? MaxIt<5>::value : MaxIt<8>::value;
+    const int nb = d.n / r;
+    t = std::max(t, (nb + it - 1) / it);
+  }
+  return t;
+}
+
+// exp(-2 pi i m / n) for m = 0..n-1, accurate to the last bit in practice:
+// angles are folded into [0, pi/4] and evaluated in long double.
+static void twiddles(int n, std::vector<double2>& w) {
+  w.resize(n);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int m = 0; m < n; m++) {
+    // reduce 8m/n into an octant index and remainder
+    long long num = 8LL * m;          // angle = 2 pi m / n = (pi/4) * (8m/n)
+    long long oct = num / n;          // octant 0..7
+    long long rem = num - oct * n;    // angle within octant = (pi/4) rem / n
+    long double x = pi / 4 * (long double)rem / (long double)n;
+    long double c = cosl(x), s = sinl(x);
+    long double cr, sr;               // cos, sin of the full angle
+    switch (oct) {
+      case 0: cr = c; sr = s; break;
+      case 1: { long double y = pi / 4 - x; cr = sinl(y); sr = cosl(y); break; }
+      case 2: cr = -s; sr = c; break;
+      case 3: { long double y = pi / 4 - x; cr = -cosl(y); sr = sinl(y); break; }
+      case 4: cr = -c; sr = -s; break;
+      case 5: { long double y = pi / 4 - x; cr = -sinl(y); sr = -cosl(y); break; }
+      case 6: cr = s; sr = -c; break;
+      default: { long double y = pi / 4 - x; cr = cosl(y); sr = -sinl(y); break; }
+    }
+    w[m] = make_double2((double)cr, -(double)sr);
+  }
+}
+
+static size_t row_adv_smem(const pqg_plan* p, int rb) {
+  return sizeof(double2) * ((size_t)p->nx + 3 * (size_t)rb * p->M);
+}
+static size_t row_batch_smem(const pqg_plan* p, int rb) {
+  return sizeof(double2) * ((size_t)p->nx + (size_t)rb * p->M);
+}
+static size_t col_smem(const pqg_plan* p, int nseq) {
+  return sizeof(double2) * ((size_t)p->ny * (1 + nseq));
+}
+
+static Geo geo(const pqg_plan* p) {
+  Geo g;
+  g.nz = p->nz; g.ny = p->ny; g.nx = p->nx; g.nk = p->nk; g.M = p->M;
+  g.scale = 1.0 / ((double)p->nx * (double)p->ny);
+  g.fx = p->fx; g.fy = p->fy;
+  g.twx = p->twx; g.twy = p->twy;
+  return g;
+}
+static Consts consts(const pqg_plan* p) {
+  Consts c;
+  c.a = p->a; c.kk = p->kk; c.ll = p->ll; c.k2l2 = p->k2l2; c.kQy = p->kQy;
+  c.Ubg = p->Ubg; c.filtr = p->filtr; c.rek = p->rek;
+  return c;
+}
+
+static int ensure_scratch(pqg_plan* p, int planes) {
+  if (planes <= p->scratch_planes) return PQG_OK;
+  if (p->scratch) return fail(PQG_ERR_STATE, "scratch already allocated");
+  const size_t bytes = sizeof(double2) * (size_t)planes * p->ny * p->nk;
+  if (cudaMalloc(&p->scratch, bytes) != cudaSuccess)
+    return fail(PQG_ERR_NOMEM, "cudaMalloc scratch failed");
+  p->scratch_planes = planes;
+  return PQG_OK;
+}
+
+static void drop_graphs(pqg_plan* p) {
+  for (auto& e : p->graphs) cudaGraphExecDestroy(e.exec);
+  p->graphs.clear();
+}
+
+static double2* dc(double* x) { return reinterpret_cast<double2*>(x); }
+static const double2* dc(const double* x) { return reinterpret_cast<const double2*>(x); }
+
+#define CHECK_LAUNCH() PQG_CUDA(cudaGetLastError())
+
+// ---------------------------------------------------------------------------
+// launch helpers (stage kernels)
+// ---------------------------------------------------------------------------
+static int launch_row_adv(pqg_plan* p, const RowAdvArgs& A0, cudaStream_t st) {
+  RowAdvArgs A = A0;
+  A.rb = p->rb;
+  A.Ubg = p->Ubg;
+  const int nrows = p->nz * p->ny;
+  const int grid = (nrows + A.rb - 1) / A.rb;
+  k_row_adv<<<grid, p->T_row, row_adv_smem(p, A.rb), st>>>(geo(p), A);
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+static int launch_row_c2r(pqg_plan* p, const double2* mix, double* phys, int nplanes, cudaStream_t st) {
+  RowBatchArgs A{};
+  A.mixsrc = mix;
+  A.phys = phys;
+  A.nrows = nplanes * p->ny;
+  A.rb = p->rb_batch;
+  const int grid = (A.nrows + A.rb - 1) / A.rb;
+  k_row_c2r<<<grid, p->T_row_batch, row_batch_smem(p, A.rb), st>>>(geo(p), A);
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+static int launch_row_r2c(pqg_plan* p, const double* phys, double2* mix, int nplanes, cudaStream_t st) {
+  RowBatchArgs A{};
+  A.physsrc = phys;
+  A.mixdst = mix;
+  A.nrows = nplanes * p->ny;
+  A.rb = p->rb_batch;
+  const int grid = (A.nrows + A.rb - 1) / A.rb;
+  k_row_r2c<<<grid, p->T_row_batch, row_batch_smem(p, A.rb), st>>>(geo(p), A);
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+template <bool INV>
+static int launch_col_batch(pqg_plan* p, const double2* src, double2* dst, int nplanes, cudaStream_t st) {
+  dim3 grid(nplanes, p->nk);
+  k_col_batch<INV><<<grid, p->T_col, col_smem(p, 1), st>>>(geo(p), src, dst);
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+static int launch_col_fused(pqg_plan* p, const FusedColArgs& A, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p->nz, p->nk, 1);
+  cfg.blockDim = dim3(p->T_col, 1, 1);
+  cfg.dynamicSmemBytes = col_smem(p, 4);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = p->nz;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PQG_CUDA(cudaLaunchKernelEx(&cfg, k_col_fused, geo(p), consts(p), A));
+  return PQG_OK;
+}
+
+static void ab_coeffs(int ablevel, double dt, double& c1, double& c2, double& c3) {
+  // pyqg/kernel.pyx:479-495
+  if (ablevel <= 0) { c1 = dt; c2 = 0.0; c3 = 0.0; }
+  else if (ablevel == 1) { c1 = 1.5 * dt; c2 = -0.5 * dt; c3 = 0.0; }
+  else { c1 = 23. / 12. * dt; c2 = -16. / 12. * dt; c3 = 5. / 12. * dt; }
+}
+
+static int set_smem_limits() {
+  static bool done = false;
+  if (done) return PQG_OK;
+  const int big = 200 * 1024;
+  PQG_CUDA(cudaFuncSetAttribute(k_row_adv, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_row_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_col_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_col_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_col_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_col_adv, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_col_ab3, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_col_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(k_col_fused, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  done = true;
+  return PQG_OK;
+}
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+#define PQG_API __attribute__((visibility("default")))
+
+extern "C" {
+
+PQG_API int pqg_version(void) { return 100; }
+
+PQG_API const char* pqg_last_error(void) { return g_last_error.c_str(); }
+
+PQG_API int pqg_plan_create(pqg_plan** out, int nz, int ny, int nx) {
+  if (!out) return fail(PQG_ERR_INVALID, "plan output pointer is NULL");
+  *out = nullptr;
+  if (nz < 1 || ny < 2 || nx < 2) return fail(PQG_ERR_INVALID, "grid sizes must be positive");
+  if (nx % 2 || ny % 2) return fail(PQG_ERR_UNSUPPORTED, "nx and ny must be even");
+  if (nx / 2 > 2048 || ny > 2048) return fail(PQG_ERR_UNSUPPORTED, "nx/2 and ny must be <= 2048");
+  if (nz > 8) return fail(PQG_ERR_UNSUPPORTED, "nz must be <= 8");
+  pqg_plan* p = new pqg_plan();
+  p->nz = nz; p->ny = ny; p->nx = nx; p->nk = nx / 2 + 1; p->M = nx / 2;
+  if (!factor(p->M, p->fx) || !factor(ny, p->fy)) {
+    delete p;
+    return fail(PQG_ERR_UNSUPPORTED, "nx/2 and ny must factor into 2, 3 and 5");
+  }
+  if (col_smem(p, 4) > 200 * 1024 || row_adv_smem(p, 1) > 200 * 1024) {
+    delete p;
+    return fail(PQG_ERR_UNSUPPORTED, "grid too large for the shared-memory kernels");
+  }
+  // block shapes: the Stockham stages need blockDim * MaxIt >= n / R
+  p->T_col = std::max(64, std::min(256, ny / 2));
+  p->T_row = std::max(64, std::min(256, p->M));
+  if (p->T_col < min_threads(p->fy)) p->T_col = std::min(1024, (min_threads(p->fy) + 31) / 32 * 32);
+  if (p->T_row < min_threads(p->fx)) p->T_row = std::min(1024, (min_threads(p->fx) + 31) / 32 * 32);
+  p->rb = std::max(1, std::min(4, 128 / p->M));
+  p->T_row_batch = p->T_row;
+  p->rb_batch = std::max(1, std::min(8, 256 / p->M));
+  if (p->T_col < min_threads(p->fy) || p->T_row < min_threads(p->fx)) {
+    delete p;
+    return fail(PQG_ERR_UNSUPPORTED, "transform too long for the block size");
+  }
+  if (const char* e = getenv("PQG_NO_GRAPHS")) p->use_graphs = (e[0] == '0');
+  int rc = set_smem_limits();
+  if (rc) { delete p; return rc; }
+
+  std::vector<double2> w;
+  const size_t nl = ny, nk = p->nk;
+  auto alloc = [&](void** ptr, size_t bytes) {
+    return cudaMalloc(ptr, bytes) == cudaSuccess && cudaMemset(*ptr, 0, bytes) == cudaSuccess;
+  };
+  bool ok = alloc((void**)&p->twx, sizeof(double2) * nx) &&
+            alloc((void**)&p->twy, sizeof(double2) * ny) &&
+            alloc((void**)&p->a, sizeof(double) * nz * nz * nl * nk) &&
+            alloc((void**)&p->kk, sizeof(double) * nk) &&
+            alloc((void**)&p->ll, sizeof(double) * nl) &&
+            alloc((void**)&p->k2l2, sizeof(double) * nl * nk) &&
+            alloc((void**)&p->kQy, sizeof(double) * nz * nk) &&
+            alloc((void**)&p->Ubg, sizeof(double) * nz) &&
+            alloc((void**)&p->filtr, sizeof(double) * nl * nk);
+  if (!ok) { pqg_plan_destroy(p); return fail(PQG_ERR_NOMEM, "cudaMalloc failed in plan_create"); }
+  twiddles(nx, w);
+  cudaMemcpy(p->twx, w.data(), sizeof(double2) * nx, cudaMemcpyHostToDevice);
+  twiddles(ny, w);
+  cudaMemcpy(p->twy, w.data(), sizeof(double2) * ny, cudaMemcpyHostToDevice);
+  rc = ensure_scratch(p, 5 * nz);
+  if (rc) { pqg_plan_destroy(p); return rc; }
+  if (cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    pqg_plan_destroy(p);
+    return fail(PQG_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  PQG_CUDA(cudaDeviceSynchronize());
+  *out = p;
+  return PQG_OK;
+}
+
+PQG_API int pqg_plan_destroy(pqg_plan* p) {
+  if (!p) return PQG_OK;
+  drop_graphs(p);
+  cudaFree(p->twx); cudaFree(p->twy); cudaFree(p->a); cudaFree(p->kk);
+  cudaFree(p->ll); cudaFree(p->k2l2); cudaFree(p->kQy); cudaFree(p->Ubg);
+  cudaFree(p->filtr); cudaFree(p->scratch);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  delete p;
+  return PQG_OK;
+}
+
+static int upload(double* dst, const double* src, size_t n) {
+  PQG_CUDA(cudaMemcpy(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice));
+  return PQG_OK;
+}
+
+static int refresh_kqy(pqg_plan* p) {
+  if (!(p->have_kk && p->have_qy)) return PQG_OK;
+  std::vector<double> t((size_t)p->nz * p->nk);
+  for (int z = 0; z < p->nz; z++)
+    for (int i = 0; i < p->nk; i++) t[(size_t)z * p->nk + i] = p->h_kk[i] * p->h_Qy[z];
+  return upload(p->kQy, t.data(), t.size());
+}
+
+PQG_API int pqg_set_wavenumbers(pqg_plan* p, const double* kk, const double* ll) {
+  if (!p || !kk || !ll) return fail(PQG_ERR_INVALID, "NULL argument");
+  drop_graphs(p);
+  p->h_kk.assign(kk, kk + p->nk);
+  p->h_ll.assign(ll, ll + p->ny);
+  p->have_kk = p->have_ll = true;
+  int rc = upload(p->kk, kk, p->nk);
+  if (!rc) rc = upload(p->ll, ll, p->ny);
+  if (rc) return rc;
+  // k2l2 = kk^2 + ll^2 (pyqg/kernel.pyx:544-546), evaluated without
+  // contraction (the library is built with -ffp-contract=off)
+  std::vector<double> t((size_t)p->ny * p->nk);
+  for (int j = 0; j < p->ny; j++)
+    for (int i = 0; i < p->nk; i++) {
+      const double a = kk[i] * kk[i];
+      const double b = ll[j] * ll[j];
+      t[(size_t)j * p->nk + i] = a + b;
+    }
+  rc = upload(p->k2l2, t.data(), t.size());
+  if (rc) return rc;
+  return refresh_kqy(p);
+}
+
+PQG_API int pqg_set_k2l2(pqg_plan* p, const double* k2l2) {
+  if (!p || !k2l2) return fail(PQG_ERR_INVALID, "NULL argument");
+  drop_graphs(p);
+  return upload(p->k2l2, k2l2, (size_t)p->ny * p->nk);
+}
+
+PQG_API int pqg_set_inversion(pqg_plan* p, const double* a) {
+  if (!p || !a) return fail(PQG_ERR_INVALID, "NULL argument");
+  drop_graphs(p);
+  return upload(p->a, a, (size_t)p->nz * p->nz * p->ny * p->nk);
+}
+
+PQG_API int pqg_set_ubg(pqg_plan* p, const double* Ubg) {
+  if (!p || !Ubg) return fail(PQG_ERR_INVALID, "NULL argument");
+  drop_graphs(p);
+  return upload(p->Ubg, Ubg, p->nz);
+}
+
+PQG_API int pqg_set_qy(pqg_plan* p, const double* Qy) {
+  if (!p || !Qy) return fail(PQG_ERR_INVALID, "NULL argument");
+  drop_graphs(p);
+  p->h_Qy.assign(Qy, Qy + p->nz);
+  p->have_qy = true;
+  return refresh_kqy(p);
+}
+
+PQG_API int pqg_set_filter(pqg_plan* p, const double* filtr) {
+  if (!p || !filtr) return fail(PQG_ERR_INVALID, "NULL argument");
+  drop_graphs(p);
+  return upload(p->filtr, filtr, (size_t)p->ny * p->nk);
+}
+
+PQG_API int pqg_set_rek(pqg_plan* p, double rek) {
+  if (!p) return fail(PQG_ERR_INVALID, "NULL argument");
+  if (rek != p->rek) drop_graphs(p);
+  p->rek = rek;
+  return PQG_OK;
+}
+
+PQG_API int pqg_rfft2(pqg_plan* p, const double* x, double* xh, int nplanes, void* stream) {
+  if (!p || !x || !xh || nplanes < 0) return fail(PQG_ERR_INVALID, "bad argument to pqg_rfft2");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int chunk = p->scratch_planes;
+  const size_t pr = (size_t)p->ny * p->nx, pc = (size_t)p->ny * p->nk;
+  for (int p0 = 0; p0 < nplanes; p0 += chunk) {
+    const int n = std::min(chunk, nplanes - p0);
+    int rc = launch_row_r2c(p, x + p0 * pr, p->scratch, n, st);
+    if (!rc) rc = launch_col_batch<false>(p, p->scratch, dc(xh) + p0 * pc, n, st);
+    if (rc) return rc;
+  }
+  return PQG_OK;
+}
+
+PQG_API int pqg_irfft2(pqg_plan* p, const double* xh, double* x, int nplanes, void* stream) {
+  if (!p || !x || !xh || nplanes < 0) return fail(PQG_ERR_INVALID, "bad argument to pqg_irfft2");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int chunk = p->scratch_planes;
+  const size_t pr = (size_t)p->ny * p->nx, pc = (size_t)p->ny * p->nk;
+  for (int p0 = 0; p0 < nplanes; p0 += chunk) {
+    const int n = std::min(chunk, nplanes - p0);
+    int rc = launch_col_batch<true>(p, dc(xh) + p0 * pc, p->scratch, n, st);
+    if (!rc) rc = launch_row_c2r(p, p->scratch, x + p0 * pr, n, st);
+    if (rc) return rc;
+  }
+  return PQG_OK;
+}
+
+PQG_API int pqg_invert(pqg_plan* p, const double* qh, double* ph, double* uh, double* vh,
+               double* u, double* v, void* stream) {
+  if (!p || !qh || !u || !v) return fail(PQG_ERR_INVALID, "NULL argument to pqg_invert");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t pc = (size_t)p->ny * p->nk;
+  double2* mU = p->scratch;
+  double2* mV = p->scratch + p->nz * pc;
+  dim3 grid(p->nz, p->nk);
+  k_col_invert<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), dc(qh), dc(ph), dc(uh), dc(vh), mU, mV);
+  CHECK_LAUNCH();
+  int rc = launch_row_c2r(p, mU, u, p->nz, st);
+  if (!rc) rc = launch_row_c2r(p, mV, v, p->nz, st);
+  return rc;
+}
+
+PQG_API int pqg_do_advection(pqg_plan* p, const double* q, const double* u, const double* v,
+                     const double* ph, double* uq, double* vq, double* uqh, double* vqh,
+                     double* dqhdt, void* stream) {
+  if (!p || !q || !u || !v || !ph || !dqhdt) return fail(PQG_ERR_INVALID, "NULL argument to pqg_do_advection");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t pc = (size_t)p->ny * p->nk;
+  RowAdvArgs A{};
+  A.physU = u; A.physV = v; A.physQ = q;
+  A.outUQ = uq; A.outVQ = vq;
+  A.mixUQ = p->scratch;
+  A.mixVQ = p->scratch + p->nz * pc;
+  int rc = launch_row_adv(p, A, st);
+  if (rc) return rc;
+  dim3 grid(p->nz, p->nk);
+  k_col_adv<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), A.mixUQ, A.mixVQ, dc(ph), dc(uqh), dc(vqh), dc(dqhdt));
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+PQG_API int pqg_do_friction(pqg_plan* p, const double* ph, double* dqhdt, void* stream) {
+  if (!p || !ph || !dqhdt) return fail(PQG_ERR_INVALID, "NULL argument to pqg_do_friction");
+  if (p->rek == 0.0) return PQG_OK;  // `if self.rek:` (pyqg/kernel.pyx:451)
+  const int n = p->ny * p->nk;
+  k_friction<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(geo(p), consts(p), dc(ph), dc(dqhdt));
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+PQG_API int pqg_do_q_forcing(pqg_plan* p, const double* dq, double* dqh, double* dqhdt, void* stream) {
+  if (!p || !dq || !dqhdt) return fail(PQG_ERR_INVALID, "NULL argument to pqg_do_q_forcing");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t pc = (size_t)p->ny * p->nk;
+  int rc = ensure_scratch(p, 4 * p->nz);
+  if (rc) return rc;
+  double2* tmp = dqh ? dc(dqh) : p->scratch + 3 * p->nz * pc;
+  rc = launch_row_r2c(p, dq, p->scratch, p->nz, st);
+  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tmp, p->nz, st);
+  if (rc) return rc;
+  const size_t n = p->nz * pc;
+  k_add_q<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(geo(p), tmp, dc(dqhdt));
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+PQG_API int pqg_do_uv_forcing(pqg_plan* p, const double* du, const double* dv, double* duh,
+                      double* dvh, double* dqhdt, void* stream) {
+  if (!p || !du || !dv || !dqhdt) return fail(PQG_ERR_INVALID, "NULL argument to pqg_do_uv_forcing");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t pc = (size_t)p->ny * p->nk;
+  int rc = ensure_scratch(p, 5 * p->nz);
+  if (rc) return rc;
+  double2* tu = duh ? dc(duh) : p->scratch + 3 * p->nz * pc;
+  double2* tv = dvh ? dc(dvh) : p->scratch + 4 * p->nz * pc;
+  rc = launch_row_r2c(p, du, p->scratch, p->nz, st);
+  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tu, p->nz, st);
+  if (!rc) rc = launch_row_r2c(p, dv, p->scratch, p->nz, st);
+  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tv, p->nz, st);
+  if (rc) return rc;
+  const size_t n = p->nz * pc;
+  k_add_uv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(geo(p), consts(p), tu, tv, dc(dqhdt));
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+PQG_API int pqg_forward_timestep(pqg_plan* p, int ablevel, double dt, double* qh, const double* dqhdt,
+                         double* dqhdt_p, double* dqhdt_pp, double* q, int rotate, void* stream) {
+  if (!p || !qh || !dqhdt || !dqhdt_p || !dqhdt_pp || !q)
+    return fail(PQG_ERR_INVALID, "NULL argument to pqg_forward_timestep");
+  cudaStream_t st = (cudaStream_t)stream;
+  double c1, c2, c3;
+  ab_coeffs(ablevel, dt, c1, c2, c3);
+  dim3 grid(p->nz, p->nk);
+  k_col_ab3<<<grid, p->T_col, col_smem(p, 1), st>>>(geo(p), consts(p), dc(qh), dc(dqhdt), dc(dqhdt_p),
+                                                     dc(dqhdt_pp), c1, c2, c3, rotate, p->scratch);
+  CHECK_LAUNCH();
+  return launch_row_c2r(p, p->scratch, q, p->nz, st);
+}
+
+// one fused step: row kernel (+ column kernel); `first` reads physical q.
+// `ev` (optional, 3 events) is recorded before the row kernel, between the
+// two kernels and after the column kernel.
+static int fused_step(pqg_plan* p, pqg_state* s, bool first, const pqg_aux* aux, cudaStream_t st,
+                      cudaEvent_t* ev = nullptr) {
+  const size_t pc = (size_t)p->ny * p->nk;
+  double2* mU = p->scratch;
+  double2* mV = p->scratch + p->nz * pc;
+  double2* mQ = p->scratch + 2 * p->nz * pc;
+  RowAdvArgs R{};
+  R.mixU = mU; R.mixV = mV;
+  if (first) R.physQ = s->q; else R.mixQ = mQ;
+  R.mixUQ = mU; R.mixVQ = mV;
+  if (aux) { R.outU = aux->u; R.outV = aux->v; R.outUQ = aux->uq; R.outVQ = aux->vq; }
+  if (ev) PQG_CUDA(cudaEventRecord(ev[0], st));
+  int rc = launch_row_adv(p, R, st);
+  if (rc) return rc;
+  if (ev) PQG_CUDA(cudaEventRecord(ev[1], st));
+  FusedColArgs C{};
+  C.qh = dc(s->qh);
+  C.dqp = dc(s->dqhdt_p);
+  C.dqpp = dc(s->dqhdt_pp);
+  C.dqout = dc(s->dqhdt_pp);
+  C.mixUQ = mU; C.mixVQ = mV;
+  C.mixU = mU; C.mixV = mV; C.mixQ = mQ;
+  if (aux) { C.ph = dc(aux->ph); C.uh = dc(aux->uh); C.vh = dc(aux->vh); C.uqh = dc(aux->uqh); C.vqh = dc(aux->vqh); }
+  ab_coeffs(s->ablevel, s->dt, C.c1, C.c2, C.c3);
+  rc = launch_col_fused(p, C, st);
+  if (rc) return rc;
+  if (ev) PQG_CUDA(cudaEventRecord(ev[2], st));
+  // history rotation by pointers (values as pyqg/kernel.pyx:509-510)
+  double* newest = s->dqhdt_pp;
+  s->dqhdt_pp = s->dqhdt_p;
+  s->dqhdt_p = newest;
+  s->dqhdt = newest;
+  s->ablevel = s->ablevel >= 2 ? 2 : s->ablevel + 1;
+  s->tc += 1;
+  s->t += s->dt;
+  return PQG_OK;
+}
+
+PQG_API int pqg_step(pqg_plan* p, pqg_state* s, int nsteps, const pqg_aux* aux, void* stream) {
+  if (!p || !s || !s->q || !s->qh || !s->dqhdt_p || !s->dqhdt_pp)
+    return fail(PQG_ERR_INVALID, "NULL argument to pqg_step");
+  if (s->dqhdt_p == s->dqhdt_pp) return fail(PQG_ERR_INVALID, "dqhdt_p and dqhdt_pp must be distinct buffers");
+  if (nsteps <= 0) return nsteps == 0 ? PQG_OK : fail(PQG_ERR_INVALID, "nsteps < 0");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t pc = (size_t)p->ny * p->nk;
+  // prologue: mixed U, V of the current qh
+  dim3 grid(p->nz, p->nk);
+  k_col_invert<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), dc(s->qh), nullptr, nullptr, nullptr,
+                                                        p->scratch, p->scratch + p->nz * pc);
+  CHECK_LAUNCH();
+  int done = 0;
+  int rc = fused_step(p, s, true, nsteps == 1 ? aux : nullptr, st);
+  if (rc) return rc;
+  done = 1;
+  // warm-up steps until AB3 (coefficients constant afterwards)
+  while (done < nsteps - 1 && s->ablevel < 2) {
+    rc = fused_step(p, s, false, nullptr, st);
+    if (rc) return rc;
+    done++;
+  }
+  // steady state: replay cached graphs of an even number of steps (the
+  // history buffers return to the same roles every two steps)
+  const int chunk = 16;
+  while (p->use_graphs && nsteps - 1 - done >= chunk) {
+    std::vector<const void*> key = {s->q, s->qh, s->dqhdt_p, s->dqhdt_pp, p->scratch, stream};
+    double c[3];
+    ab_coeffs(2, s->dt, c[0], c[1], c[2]);
+    GraphEntry* hit = nullptr;
+    for (auto& e : p->graphs)
+      if (e.key == key && e.nsteps == chunk && e.c[0] == c[0] && e.c[1] == c[1] && e.c[2] == c[2]) hit = &e;
+    pqg_state s2 = *s;
+    if (!hit) {
+      cudaGraph_t graph;
+      PQG_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < chunk; i++) {
+        rc = fused_step(p, &s2, false, nullptr, p->cap_stream);
+        if (rc) {
+          cudaStreamEndCapture(p->cap_stream, &graph);
+          if (graph) cudaGraphDestroy(graph);
+          return rc;
+        }
+      }
+      PQG_CUDA(cudaStreamEndCapture(p->cap_stream, &graph));
+      GraphEntry e;
+      e.key = key;
+      e.nsteps = chunk;
+      e.c[0] = c[0]; e.c[1] = c[1]; e.c[2] = c[2];
+      cudaError_t ie = cudaGraphInstantiate(&e.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) return fail(PQG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+      if (p->graphs.size() >= 8) {
+        cudaGraphExecDestroy(p->graphs.front().exec);
+        p->graphs.erase(p->graphs.begin());
+      }
+      p->graphs.push_back(e);
+      hit = &p->graphs.back();
+    } else {
+      for (int i = 0; i < chunk; i++) {
+        double* newest = s2.dqhdt_pp;
+        s2.dqhdt_pp = s2.dqhdt_p;
+        s2.dqhdt_p = newest;
+        s2.dqhdt = newest;
+        s2.tc += 1;
+        s2.t += s2.dt;
+      }
+    }
+    PQG_CUDA(cudaGraphLaunch(hit->exec, st));
+    *s = s2;
+    done += chunk;
+  }
+  while (done < nsteps) {
+    rc = fused_step(p, s, false, done == nsteps - 1 ? aux : nullptr, st);
+    if (rc) return rc;
+    done++;
+  }
+  // epilogue: physical q of the final state
+  return launch_row_c2r(p, p->scratch + 2 * p->nz * pc, s->q, p->nz, st);
+}
+
+PQG_API int pqg_step_profile(pqg_plan* p, pqg_state* s, int nsteps, double* ms, int* counts,
+                             void* stream) {
+  if (!p || !s || !ms || !counts || nsteps < 1) return fail(PQG_ERR_INVALID, "bad argument to pqg_step_profile");
+  if (s->dqhdt_p == s->dqhdt_pp) return fail(PQG_ERR_INVALID, "dqhdt_p and dqhdt_pp must be distinct buffers");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t pc = (size_t)p->ny * p->nk;
+  dim3 grid(p->nz, p->nk);
+  k_col_invert<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), dc(s->qh), nullptr, nullptr, nullptr,
+                                                        p->scratch, p->scratch + p->nz * pc);
+  CHECK_LAUNCH();
+  std::vector<cudaEvent_t> ev(3 * nsteps);
+  for (auto& e : ev) PQG_CUDA(cudaEventCreate(&e));
+  int rc = PQG_OK;
+  for (int i = 0; i < nsteps && !rc; i++) rc = fused_step(p, s, i == 0, nullptr, st, &ev[3 * i]);
+  if (!rc) rc = launch_row_c2r(p, p->scratch + 2 * p->nz * pc, s->q, p->nz, st);
+  if (!rc) {
+    PQG_CUDA(cudaStreamSynchronize(st));
+    ms[0] = ms[1] = 0.0;
+    for (int i = 0; i < nsteps; i++) {
+      float a = 0.f, b = 0.f;
+      cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]);
+      cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]);
+      ms[0] += a;
+      ms[1] += b;
+    }
+    counts[0] = counts[1] = nsteps;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,575 @@
+"""GPU-backed drop-in for pyqg's ``PseudoSpectralKernel``.
+
+Mirrors the constructor, properties and methods of the reference Cython class
+(``pyqg/kernel.pyx:32-637``).  Every field lives in device memory (torch
+CUDA tensors used only as allocations); the arithmetic runs in the CUDA
+library ``libpyqg_gb300.so`` through its C ABI.  There is no CPU path: a
+kernel cannot be constructed without a CUDA device and the built library.
+
+Aliasing views.  The reference hands out numpy views of its buffers and code
+writes through them (``m.u[0] = ...``, ``m.dqhdt[:] = ...``).  Here a getter
+downloads the field into a persistent pinned host array (the same array
+object every time) and returns it; before the next device operation every
+array handed out since the last operation is uploaded back, so writes
+through the returned array reach the device.  Arrays held across a device
+operation are refreshed by the next getter call, not automatically.
+
+History buffers.  ``dqhdt``, ``dqhdt_p`` and ``dqhdt_pp`` are three logical
+roles over three device buffers.  The reference shifts the history by
+copying (``pyqg/kernel.pyx:509-510``); here roles are re-pointed instead and
+a role that shares its buffer with another is given a free buffer before it
+is written (copy-on-write).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_PHYS = ("q", "u", "v", "uq", "vq", "dq", "du", "dv")
+_SPEC = ("qh", "ph", "uh", "vh", "uqh", "vqh", "dqh", "duh", "dvh")
+_TEND = ("dqhdt", "dqhdt_p", "dqhdt_pp")
+_AUX = ("ph", "uh", "vh", "u", "v", "uq", "vq", "uqh", "vqh")
+
+
+def _check_array(x, dtype, ndim, name):
+    """Typed-buffer checks of the reference setters (np.ndarray[T, ndim=N])."""
+    if not isinstance(x, np.ndarray):
+        raise TypeError("%s must be a numpy.ndarray, got %s" % (name, type(x).__name__))
+    if x.dtype != dtype:
+        raise ValueError("Buffer dtype mismatch for %s: expected %s but got %s"
+                         % (name, np.dtype(dtype), x.dtype))
+    if x.ndim != ndim:
+        raise ValueError("Buffer has wrong number of dimensions for %s "
+                         "(expected %d, got %d)" % (name, ndim, x.ndim))
+    return x
+
+
+class PseudoSpectralKernel:
+    """Drop-in replacement of ``pyqg.kernel.PseudoSpectralKernel``."""
+
+    def __new__(cls, *args, **kwargs):
+        self = super().__new__(cls)
+        # properties may be set before __init__ (pyqg/layered_model.py:121)
+        self.__dict__["_pre"] = {}
+        self.__dict__["_plan"] = None
+        return self
+
+    def __init__(self, nz, ny, nx, fftw_num_threads=1, has_q_param=0,
+                 has_uv_param=0):
+        if not torch.cuda.is_available():
+            raise RuntimeError("pyqg_gb300 needs a CUDA device; none is visible")
+        L = _lib.lib()
+        self.nz, self.ny, self.nx = int(nz), int(ny), int(nx)
+        self.nl = self.ny
+        self.nk = int(self.nx / 2 + 1)
+        self.num_threads = fftw_num_threads
+        self._L = L
+        self._device = torch.device("cuda", torch.cuda.current_device())
+        self._stream = torch.cuda.current_stream(self._device)
+        plan = ctypes.c_void_p()
+        _lib.check(L.pqg_plan_create(ctypes.byref(plan), self.nz, self.ny, self.nx))
+        self._plan = plan
+        dev = self._device
+        shp_r = (self.nz, self.ny, self.nx)
+        shp_c = (self.nz, self.nl, self.nk)
+        self._d = {}
+        names_r = ["q", "u", "v", "uq", "vq"]
+        names_c = ["qh", "ph", "uh", "vh", "uqh", "vqh"]
+        self._has_uv = bool(has_uv_param)
+        self._has_q = bool(has_q_param)
+        if self._has_uv:
+            names_r += ["du", "dv"]
+            names_c += ["duh", "dvh"]
+        if self._has_q:
+            names_r += ["dq"]
+            names_c += ["dqh"]
+        for n in names_r:
+            self._d[n] = torch.zeros(shp_r, dtype=torch.float64, device=dev)
+        for n in names_c:
+            self._d[n] = torch.zeros(shp_c, dtype=torch.complex128, device=dev)
+        self._tend = [torch.zeros(shp_c, dtype=torch.complex128, device=dev)
+                      for _ in range(3)]
+        self._role = {"dqhdt": 0, "dqhdt_p": 1, "dqhdt_pp": 2}
+        self._shadow = {}       # name -> (pinned tensor, numpy view)
+        self._current = set()   # names whose host array holds the latest value
+        # time (pyqg/kernel.pyx:190-194)
+        self._dt = 0.0
+        self._t = 0.0
+        self._tc = 0
+        self._ablevel = 0
+        self._rek = 0.0
+        # constants (pyqg/kernel.pyx:127-132)
+        self._a = np.zeros((self.nz, self.nz, self.nl, self.nk), np.complex128)
+        self._kk = np.zeros(self.nk)
+        self._ll = np.zeros(self.nl)
+        self._ik = np.zeros(self.nk, np.complex128)
+        self._il = np.zeros(self.nl, np.complex128)
+        self.__dict__["_k2l2_arr"] = np.zeros((self.nl, self.nk))
+        self._Ubg = None
+        self._Qy = None
+        self._ikQy = None
+        self._filtr = None
+        zero_u = np.zeros(self.nz)
+        _lib.check(L.pqg_set_ubg(plan, zero_u.ctypes.data))
+        _lib.check(L.pqg_set_qy(plan, zero_u.ctypes.data))
+        # apply properties set before __init__
+        pre = self.__dict__.pop("_pre")
+        for name, val in pre.items():
+            setattr(self, name, val)
+
+    def __del__(self):
+        plan = self.__dict__.get("_plan")
+        if plan is not None and plan.value:
+            try:
+                torch.cuda.synchronize(self._device)
+                self._L.pqg_plan_destroy(plan)
+            except Exception:
+                pass
+            self.__dict__["_plan"] = None
+
+    # ------------------------------------------------------------------
+    # buffer plumbing
+    # ------------------------------------------------------------------
+    def _ready(self):
+        return self.__dict__.get("_plan") is not None
+
+    def _sp(self):
+        return ctypes.c_void_p(self._stream.cuda_stream)
+
+    def _buf(self, name):
+        if name in _TEND:
+            return self._tend[self._role[name]]
+        try:
+            return self._d[name]
+        except KeyError:
+            raise AttributeError("%s is not allocated (no matching "
+                                 "parameterization)" % name) from None
+
+    def _ptr(self, name):
+        return self._buf(name).data_ptr()
+
+    def _host(self, name):
+        sh = self._shadow.get(name)
+        if sh is None:
+            t = torch.empty(self._buf(name).shape, dtype=self._buf(name).dtype,
+                            pin_memory=True)
+            sh = (t, t.numpy())
+            self._shadow[name] = sh
+        return sh
+
+    def _get(self, name):
+        """Download (once per device update) and return the host array."""
+        buf = self._buf(name)
+        t, arr = self._host(name)
+        if name not in self._current:
+            with torch.cuda.stream(self._stream):
+                t.copy_(buf, non_blocking=True)
+            self._stream.synchronize()
+            self._current.add(name)
+        return arr
+
+    def _sync_in(self):
+        """Upload every host array handed out since the last device update."""
+        if not self._current:
+            return
+        for name in list(self._current):
+            if name in _TEND:
+                self._own(name, copy=False)
+            t, _ = self._shadow[name]
+            with torch.cuda.stream(self._stream):
+                self._buf(name).copy_(t)
+        self._current.clear()
+
+    def _shared(self, role):
+        i = self._role[role]
+        return sum(1 for v in self._role.values() if v == i) > 1
+
+    def _own(self, role, copy):
+        """Give `role` a buffer of its own (copy-on-write when `copy`)."""
+        if not self._shared(role):
+            return
+        used = set(self._role.values())
+        j = next(i for i in range(3) if i not in used)
+        if copy:
+            with torch.cuda.stream(self._stream):
+                self._tend[j].copy_(self._tend[self._role[role]])
+        self._role[role] = j
+
+    def _invalidate(self, *names):
+        for n in names:
+            self._current.discard(n)
+
+    def _upload(self, name, arr):
+        t, host = self._host(name)
+        host[...] = arr
+        with torch.cuda.stream(self._stream):
+            self._buf(name).copy_(t)
+        self._current.discard(name)
+
+    # ------------------------------------------------------------------
+    # transforms (pyqg/kernel.pyx:245-267,291-309)
+    # ------------------------------------------------------------------
+    def _device_rfft2(self, x):
+        """Device real field (n, ny, nx) float64 -> new (n, nl, nk) complex."""
+        x = x.contiguous()
+        out = torch.empty((x.shape[0], self.nl, self.nk), dtype=torch.complex128,
+                          device=self._device)
+        _lib.check(self._L.pqg_rfft2(self._plan, x.data_ptr(), out.data_ptr(),
+                                     x.shape[0], self._sp()))
+        return out
+
+    def _device_irfft2(self, xh):
+        xh = xh.contiguous()
+        out = torch.empty((xh.shape[0], self.ny, self.nx), dtype=torch.float64,
+                          device=self._device)
+        _lib.check(self._L.pqg_irfft2(self._plan, xh.data_ptr(), out.data_ptr(),
+                                      xh.shape[0], self._sp()))
+        return out
+
+    def fft(self, v):
+        """Forward transform of a real (n, ny, nx) field; returns a new array.
+        numpy input -> numpy output, CUDA tensor input -> CUDA tensor output."""
+        if isinstance(v, torch.Tensor):
+            return self._device_rfft2(v.to(self._device, torch.float64).reshape(-1, self.ny, self.nx))
+        v = np.asarray(v)
+        if v.dtype != np.float64:
+            raise ValueError("Buffer dtype mismatch, expected 'double' but got %s" % v.dtype)
+        if v.ndim != 3:
+            raise ValueError("Buffer has wrong number of dimensions (expected 3, got %d)" % v.ndim)
+        v = self._planes(v)
+        with torch.cuda.stream(self._stream):
+            d = torch.from_numpy(np.ascontiguousarray(v)).to(self._device)
+            out = self._device_rfft2(d).cpu()
+        return out.numpy()
+
+    def _planes(self, v):
+        """A single plane is broadcast over the nz layers, as the reference
+        does when copying it into its (nz, ...) transform buffer."""
+        if v.shape[0] == 1 and self.nz > 1:
+            v = np.broadcast_to(v, (self.nz,) + v.shape[1:])
+        return v
+
+    def ifft(self, v):
+        """Inverse transform of a complex (n, nl, nk) field; returns a new array."""
+        if isinstance(v, torch.Tensor):
+            return self._device_irfft2(v.to(self._device, torch.complex128).reshape(-1, self.nl, self.nk))
+        v = np.asarray(v)
+        if v.dtype != np.complex128:
+            raise ValueError("Buffer dtype mismatch, expected 'double complex' but got %s" % v.dtype)
+        if v.ndim != 3:
+            raise ValueError("Buffer has wrong number of dimensions (expected 3, got %d)" % v.ndim)
+        v = self._planes(v)
+        with torch.cuda.stream(self._stream):
+            d = torch.from_numpy(np.ascontiguousarray(v)).to(self._device)
+            out = self._device_irfft2(d).cpu()
+        return out.numpy()
+
+    # ------------------------------------------------------------------
+    # stages (pyqg/kernel.pyx:312-526)
+    # ------------------------------------------------------------------
+    def _invert(self):
+        self._sync_in()
+        _lib.check(self._L.pqg_invert(
+            self._plan, self._ptr("qh"), self._ptr("ph"), self._ptr("uh"),
+            self._ptr("vh"), self._ptr("u"), self._ptr("v"), self._sp()))
+
+    def _do_advection(self):
+        self._sync_in()
+        self._own("dqhdt", copy=False)
+        _lib.check(self._L.pqg_do_advection(
+            self._plan, self._ptr("q"), self._ptr("u"), self._ptr("v"),
+            self._ptr("ph"), self._ptr("uq"), self._ptr("vq"), self._ptr("uqh"),
+            self._ptr("vqh"), self._ptr("dqhdt"), self._sp()))
+
+    def _do_friction(self):
+        self._sync_in()
+        if self._rek:
+            self._own("dqhdt", copy=True)
+            _lib.check(self._L.pqg_do_friction(self._plan, self._ptr("ph"),
+                                               self._ptr("dqhdt"), self._sp()))
+
+    def _to_device_field(self, name, x):
+        """Copy a parameterization output into device buffer `name`."""
+        dst = self._buf(name)
+        with torch.cuda.stream(self._stream):
+            if isinstance(x, torch.Tensor):
+                dst.copy_(x.reshape(dst.shape))
+            else:
+                x = np.asarray(x, dtype=np.float64)
+                if x.shape != tuple(dst.shape):
+                    x = np.broadcast_to(x, dst.shape)
+                dst.copy_(torch.from_numpy(np.ascontiguousarray(x)))
+
+    def _do_q_subgrid_parameterization(self):
+        dq = self.q_parameterization(self)
+        self._sync_in()
+        self._to_device_field("dq", dq)
+        self._own("dqhdt", copy=True)
+        _lib.check(self._L.pqg_do_q_forcing(self._plan, self._ptr("dq"),
+                                            self._ptr("dqh"), self._ptr("dqhdt"),
+                                            self._sp()))
+
+    def _do_uv_subgrid_parameterization(self):
+        res = self.uv_parameterization(self)
+        du, dv = res[0], res[1]
+        self._sync_in()
+        self._to_device_field("du", du)
+        self._to_device_field("dv", dv)
+        self._own("dqhdt", copy=True)
+        _lib.check(self._L.pqg_do_uv_forcing(
+            self._plan, self._ptr("du"), self._ptr("dv"), self._ptr("duh"),
+            self._ptr("dvh"), self._ptr("dqhdt"), self._sp()))
+
+    def _forward_timestep(self):
+        """Filtered FE/AB2/AB3 update and q = irfft2(qh)
+        (pyqg/kernel.pyx:467-526)."""
+        self._sync_in()
+        _lib.check(self._L.pqg_forward_timestep(
+            self._plan, self._ablevel, self._dt, self._ptr("qh"),
+            self._ptr("dqhdt"), self._ptr("dqhdt_p"), self._ptr("dqhdt_pp"),
+            self._ptr("q"), 0, self._sp()))
+        # history shift by roles: pp <- p, p <- dqhdt (dqhdt keeps its value)
+        self._role["dqhdt_pp"] = self._role["dqhdt_p"]
+        self._role["dqhdt_p"] = self._role["dqhdt"]
+        self._ablevel = min(self._ablevel + 1, 2)
+        self._tc += 1
+        self._t += self._dt
+
+    def _step_fused(self, nsteps):
+        """Advance `nsteps` whole steps (no parameterization hooks) with the
+        fused two-kernel step replayed from CUDA graphs; leaves every field
+        as the stage-by-stage path would."""
+        if nsteps <= 0:
+            return
+        self._sync_in()
+        if self._role["dqhdt_p"] == self._role["dqhdt_pp"]:
+            self._own("dqhdt_pp", copy=True)
+        st = _lib.State(self._ptr("q"), self._ptr("qh"), self._ptr("dqhdt"),
+                        self._ptr("dqhdt_p"), self._ptr("dqhdt_pp"),
+                        self._ablevel, self._tc, self._t, self._dt)
+        aux = _lib.Aux(*[self._ptr(n) for n in _AUX])
+        _lib.check(self._L.pqg_step(self._plan, ctypes.byref(st), int(nsteps),
+                                    ctypes.byref(aux), self._sp()))
+        idx = {b.data_ptr(): i for i, b in enumerate(self._tend)}
+        self._role = {"dqhdt": idx[st.dqhdt], "dqhdt_p": idx[st.dqhdt_p],
+                      "dqhdt_pp": idx[st.dqhdt_pp]}
+        self._ablevel = st.ablevel
+        self._tc = st.tc
+        self._t = st.t
+
+    # ------------------------------------------------------------------
+    # properties (pyqg/kernel.pyx:528-637)
+    # ------------------------------------------------------------------
+    def __setattr__(self, name, value):
+        # before __init__ only record the properties the reference lets
+        # subclasses set early (plain attributes pass through)
+        if name in _PRE_INIT and not self._ready():
+            self.__dict__["_pre"][name] = value
+            return
+        object.__setattr__(self, name, value)
+
+    @property
+    def dt(self):
+        return self._dt
+
+    @dt.setter
+    def dt(self, dt):
+        self._dt = float(dt)
+        self._ablevel = 0  # reset timestepping to forward Euler (:531-534)
+
+    @property
+    def t(self):
+        return self._t
+
+    @property
+    def tc(self):
+        return self._tc
+
+    @property
+    def ablevel(self):
+        return self._ablevel
+
+    @property
+    def rek(self):
+        return self._rek
+
+    @rek.setter
+    def rek(self, rek):
+        self._rek = float(rek)
+        _lib.check(self._L.pqg_set_rek(self._plan, self._rek))
+
+    @property
+    def kk(self):
+        return self._kk
+
+    @kk.setter
+    def kk(self, k):
+        _check_array(k, np.float64, 1, "kk")
+        self._kk = np.ascontiguousarray(k)
+        self._ik = 1j * self._kk
+        self._push_wavenumbers()
+
+    @property
+    def ll(self):
+        return self._ll
+
+    @ll.setter
+    def ll(self, l):
+        _check_array(l, np.float64, 1, "ll")
+        self._ll = np.ascontiguousarray(l)
+        self._il = 1j * self._ll
+        self._push_wavenumbers()
+
+    def _push_wavenumbers(self):
+        kk = np.ascontiguousarray(self._kk[: self.nk], dtype=np.float64)
+        ll = np.ascontiguousarray(self._ll[: self.nl], dtype=np.float64)
+        self.__dict__["_k2l2_arr"] = kk[np.newaxis, :] ** 2 + ll[:, np.newaxis] ** 2
+        _lib.check(self._L.pqg_set_wavenumbers(self._plan, kk.ctypes.data,
+                                               ll.ctypes.data))
+        if self._Qy is not None:
+            self._ikQy = 1j * (self._kk[np.newaxis, :] * self._Qy[:, np.newaxis])
+
+    @property
+    def _k2l2(self):
+        return self.__dict__["_k2l2_arr"]
+
+    @_k2l2.setter
+    def _k2l2(self, v):
+        v = np.ascontiguousarray(_check_array(v, np.float64, 2, "_k2l2"))
+        self.__dict__["_k2l2_arr"] = v
+        _lib.check(self._L.pqg_set_k2l2(self._plan, v.ctypes.data))
+
+    @property
+    def _ik(self):
+        return self.__dict__["_ik_arr"]
+
+    @_ik.setter
+    def _ik(self, v):
+        self.__dict__["_ik_arr"] = v
+
+    @property
+    def _il(self):
+        return self.__dict__["_il_arr"]
+
+    @_il.setter
+    def _il(self, v):
+        self.__dict__["_il_arr"] = v
+
+    @property
+    def _ikQy(self):
+        return self.__dict__.get("_ikQy_arr")
+
+    @_ikQy.setter
+    def _ikQy(self, v):
+        self.__dict__["_ikQy_arr"] = v
+
+    @property
+    def a(self):
+        return self._a
+
+    @a.setter
+    def a(self, b):
+        _check_array(b, np.float64, 4, "a")
+        self._a[:] = b.astype(np.complex128)
+        ar = np.ascontiguousarray(self._a.real)
+        _lib.check(self._L.pqg_set_inversion(self._plan, ar.ctypes.data))
+
+    @property
+    def Ubg(self):
+        return self._Ubg
+
+    @Ubg.setter
+    def Ubg(self, U):
+        _check_array(U, np.float64, 1, "Ubg")
+        self._Ubg = U
+        u = np.zeros(self.nz)
+        u[: min(self.nz, U.size)] = U[: self.nz]
+        _lib.check(self._L.pqg_set_ubg(self._plan, u.ctypes.data))
+
+    @property
+    def Qy(self):
+        return self._Qy
+
+    @Qy.setter
+    def Qy(self, Qy):
+        _check_array(Qy, np.float64, 1, "Qy")
+        self._Qy = Qy
+        self._ikQy = 1j * (np.asarray(self._kk)[np.newaxis, :] *
+                           np.asarray(Qy)[:, np.newaxis])
+        q = np.zeros(self.nz)
+        q[: min(self.nz, Qy.size)] = Qy[: self.nz]
+        _lib.check(self._L.pqg_set_qy(self._plan, q.ctypes.data))
+
+    @property
+    def filtr(self):
+        return self._filtr
+
+    @filtr.setter
+    def filtr(self, f):
+        f = np.asarray(f, dtype=np.float64)
+        if f.ndim != 2:
+            raise ValueError("filtr must be 2-D (nl, nk)")
+        self._filtr = np.ascontiguousarray(np.broadcast_to(f, (self.nl, self.nk)))
+        _lib.check(self._L.pqg_set_filter(self._plan, self._filtr.ctypes.data))
+
+    # -- state ------------------------------------------------------------
+    @property
+    def q(self):
+        return self._get("q")
+
+    @q.setter
+    def q(self, b):
+        _check_array(b, np.float64, 3, "q")
+        if b.shape != (self.nz, self.ny, self.nx):
+            raise ValueError("q has shape %s, expected %s"
+                             % (b.shape, (self.nz, self.ny, self.nx)))
+        self._sync_in()
+        self._upload("q", b)
+        _lib.check(self._L.pqg_rfft2(self._plan, self._ptr("q"), self._ptr("qh"),
+                                     self.nz, self._sp()))
+
+    @property
+    def qh(self):
+        return self._get("qh")
+
+    @qh.setter
+    def qh(self, b):
+        _check_array(b, np.complex128, 3, "qh")
+        if b.shape != (self.nz, self.nl, self.nk):
+            raise ValueError("qh has shape %s, expected %s"
+                             % (b.shape, (self.nz, self.nl, self.nk)))
+        self._sync_in()
+        self._upload("qh", b)
+        _lib.check(self._L.pqg_irfft2(self._plan, self._ptr("qh"), self._ptr("q"),
+                                      self.nz, self._sp()))
+
+    @property
+    def ufull(self):
+        return self._get("u") + np.asarray(self._Ubg)[:, np.newaxis, np.newaxis]
+
+    @property
+    def vfull(self):
+        return self._get("v")
+
+    # -- device views (no host copy): for GPU-side parameterizations -------
+    def device_field(self, name):
+        """The device tensor holding field `name` (read it, do not keep it
+        across steps: history buffers change roles)."""
+        self._sync_in()
+        return self._buf(name)
+
+
+def _field_property(name):
+    def getter(self):
+        return self._get(name)
+    getter.__name__ = name
+    return property(getter)
+
+
+for _n in ("ph", "u", "v", "uh", "vh", "uq", "vq", "uqh", "vqh", "dqh", "duh",
+           "dvh", "dqhdt", "dqhdt_p", "dqhdt_pp"):
+    setattr(PseudoSpectralKernel, _n, _field_property(_n))
+
+_PRE_INIT = ("Ubg", "Qy", "a", "kk", "ll", "filtr", "rek", "dt", "q", "qh")

@@ -1,0 +1,479 @@
+"""Generic pseudo-spectral model on the GB300 kernel.
+
+Same constructor, loop and diagnostics API as ``pyqg.Model``
+(``pyqg/model.py:22-862``); the time step runs in the CUDA library through
+:class:`~pyqg_gb300.kernel.PseudoSpectralKernel`.
+
+``_step_forward`` keeps the reference's stage order (``pyqg/model.py:406-436``).
+When nothing observes the intermediate state of a step (no parameterization
+hook, no diagnostics due, no subclass overriding a stage), the step runs as
+the fused two-kernel step instead, and ``run`` / ``run_with_snapshots`` hand
+whole stretches of such steps to the CUDA library at once.  Both paths give
+bit-identical states.
+"""
+import logging
+import warnings
+
+import numpy as np
+
+from .errors import DiagnosticNotFilledError
+from .kernel import PseudoSpectralKernel
+
+__all__ = ["Model"]
+
+_MAX_BATCH = 4096
+
+
+def grid_constants(nx, ny, L, W):
+    """Spatial and spectral grids (``pyqg/model.py:446-482``).
+
+    Note ``ll`` is built from ``nx`` as in the reference (square grids)."""
+    g = {}
+    g["x"], g["y"] = np.meshgrid(np.arange(0.5, nx, 1.) / nx * L,
+                                 np.arange(0.5, ny, 1.) / ny * W)
+    g["dk"] = 2. * np.pi / L
+    g["dl"] = 2. * np.pi / W
+    nk = int(nx / 2 + 1)
+    g["ll"] = g["dl"] * np.append(np.arange(0., nx / 2), np.arange(-nx / 2, 0.))
+    g["kk"] = g["dk"] * np.arange(0., nk)
+    g["k"], g["l"] = np.meshgrid(g["kk"], g["ll"])
+    g["ik"] = 1j * g["k"]
+    g["il"] = 1j * g["l"]
+    g["dx"] = L / nx
+    g["dy"] = W / ny
+    g["M"] = nx * ny
+    g["wv2"] = g["k"] ** 2 + g["l"] ** 2
+    g["wv"] = np.sqrt(g["wv2"])
+    nonzero = g["wv2"] != 0.
+    g["wv2i"] = np.zeros_like(g["wv2"])
+    g["wv2i"][nonzero] = g["wv2"][nonzero] ** -1
+    return g
+
+
+def spectral_filter(k, l, dx, dy, filterfac):
+    """Exponential filter of Arbic & Flierl (2003) (``pyqg/model.py:496-503``):
+    1 below the cutoff 0.65 pi (grid units), exp(-filterfac (k* - c)^4) above."""
+    cphi = 0.65 * np.pi
+    wvx = np.sqrt((k * dx) ** 2. + (l * dy) ** 2.)
+    filtr = np.exp(-filterfac * (wvx - cphi) ** 4.)
+    filtr[wvx <= cphi] = 1.
+    return filtr
+
+
+class Model(PseudoSpectralKernel):
+    """A generic pseudo-spectral inversion model (see ``pyqg.Model``).
+
+    Subclasses provide ``_initialize_background``,
+    ``_initialize_inversion_matrix``, ``_initialize_forcing``, ``_calc_cfl``
+    and ``_calc_ke``.
+    """
+
+    def __init__(self, nz=1, nx=64, ny=None, L=1e6, W=None, dt=7200.,
+                 twrite=1000., tmax=1576800000., tavestart=315360000.,
+                 taveint=86400., useAB2=False, rek=5.787e-7, filterfac=23.6,
+                 f=None, g=9.81, q_parameterization=None,
+                 uv_parameterization=None, parameterization=None,
+                 diagnostics_list='all', ntd=1, log_level=1, logfile=None):
+        ny = nx if ny is None else ny
+        W = L if W is None else W
+
+        # infer the hook of an explicit parameterization object
+        # (pyqg/model.py:203-212)
+        if parameterization is not None:
+            kind = getattr(parameterization, "parameterization_type", None)
+            if kind == "uv_parameterization":
+                assert uv_parameterization is None
+                uv_parameterization = parameterization
+            elif kind == "q_parameterization":
+                assert q_parameterization is None
+                q_parameterization = parameterization
+            else:
+                raise ValueError(f"unknown parameterization type {kind}")
+
+        PseudoSpectralKernel.__init__(
+            self, nz, ny, nx, ntd,
+            has_q_param=int(q_parameterization is not None),
+            has_uv_param=int(uv_parameterization is not None))
+
+        self.L, self.W = L, W
+        self.dt = dt
+        self.twrite = twrite
+        self.tmax = tmax
+        self.tavestart = tavestart
+        self.taveint = taveint
+        self.logfile = logfile
+        self.log_level = log_level
+        self.useAB2 = useAB2   # stored, unused by the step (as the reference)
+        self.ntd = ntd
+        self.rek = rek
+        self.filterfac = filterfac
+        self.g = g
+        if f:
+            self.f = f
+            self.f2 = f ** 2
+        self.q_parameterization = q_parameterization
+        self.uv_parameterization = uv_parameterization
+
+        self._initialize_logger()
+        self._initialize_grid()
+        self._initialize_background()
+        self._initialize_forcing()
+        self._initialize_filter()
+        self._initialize_time()
+        self._initialize_inversion_matrix()
+        self._initialize_diagnostics(diagnostics_list)
+
+    # ------------------------------------------------------------------
+    # time loop
+    # ------------------------------------------------------------------
+    def run_with_snapshots(self, tsnapstart=0., tsnapint=432000.):
+        """Run the model, yielding the time every `tsnapint` seconds of model
+        time once ``t >= tsnapstart``."""
+        tsnapints = np.ceil(tsnapint / self.dt)
+        while self.t < self.tmax:
+            stop = lambda t, tc: t >= tsnapstart and (tc % tsnapints) == 0
+            self._advance(stop)
+            if self.t >= tsnapstart and (self.tc % tsnapints) == 0:
+                yield self.t
+
+    def run(self):
+        """Run the model until ``t >= tmax``."""
+        while self.t < self.tmax:
+            self._advance(lambda t, tc: False)
+
+    def _advance(self, stop_after):
+        """One step, or a batch of fusable steps ending before the next
+        observation point (diagnostics, status output, `stop_after`)."""
+        n = self._fusable_run_length(stop_after)
+        if n <= 1:
+            self._step_forward()
+        else:
+            self._step_fused(n)
+            self._print_status()
+
+    def _fusable(self):
+        """True when no code outside this library observes the inside of a
+        step: no hooks, and no stage overridden by a user subclass."""
+        if self.q_parameterization is not None or self.uv_parameterization is not None:
+            return False
+        cls = type(self)
+        for name in ("_invert", "_do_advection", "_do_friction",
+                     "_forward_timestep", "_do_external_forcing",
+                     "_step_forward", "_calc_diagnostics"):
+            impl = getattr(cls, name)
+            if getattr(impl, "__module__", "").split(".")[0] != "pyqg_gb300":
+                return False
+        return True
+
+    def _diagnostics_due(self, t, tc):
+        """Whether ``_calc_diagnostics`` fires at the start of a step at
+        (t, tc) (``pyqg/model.py:577-580``)."""
+        return (t >= self.dt) and (t >= self.tavestart) and (tc % self.taveints == 0)
+
+    def _status_due(self, tc):
+        return bool(self.log_level) and (tc % self.twrite) == 0
+
+    def _fusable_run_length(self, stop_after=lambda t, tc: False):
+        if not self._fusable():
+            return 0
+        t, tc, dt = self.t, self.tc, self.dt
+        n = 0
+        while t < self.tmax and n < _MAX_BATCH:
+            if self._diagnostics_due(t, tc):
+                break
+            t = t + dt
+            tc = tc + 1
+            n += 1
+            if self._status_due(tc) or stop_after(t, tc):
+                break
+        return n
+
+    def _step_forward(self):
+        if (self._fusable() and not self._diagnostics_due(self.t, self.tc)):
+            self._step_fused(1)
+            self._print_status()
+            return
+        # stage-by-stage path (pyqg/model.py:406-436)
+        self._invert()
+        self._do_advection()
+        self._do_friction()
+        self._do_external_forcing()
+        if self.uv_parameterization is not None:
+            self._do_uv_subgrid_parameterization()
+        if self.q_parameterization is not None:
+            self._do_q_subgrid_parameterization()
+        self._calc_diagnostics()
+        self._forward_timestep()
+        self._print_status()
+
+    # ------------------------------------------------------------------
+    # initialization
+    # ------------------------------------------------------------------
+    def _initialize_time(self):
+        self.taveints = np.ceil(self.taveint / self.dt)
+
+    def _initialize_grid(self):
+        g = grid_constants(self.nx, self.ny, self.L, self.W)
+        self.x, self.y = g["x"], g["y"]
+        self.dk, self.dl = g["dk"], g["dl"]
+        self.ll = g["ll"]
+        self.kk = g["kk"]
+        self.k, self.l = g["k"], g["l"]
+        self.ik, self.il = g["ik"], g["il"]
+        self.dx, self.dy = g["dx"], g["dy"]
+        self.M = g["M"]
+        self.wv2, self.wv, self.wv2i = g["wv2"], g["wv"], g["wv2i"]
+
+    def _initialize_background(self):
+        raise NotImplementedError('needs to be implemented by Model subclass')
+
+    def _initialize_inversion_matrix(self):
+        raise NotImplementedError('needs to be implemented by Model subclass')
+
+    def _initialize_forcing(self):
+        raise NotImplementedError('needs to be implemented by Model subclass')
+
+    def _initialize_filter(self):
+        self.filtr = spectral_filter(self.k, self.l, self.dx, self.dy, self.filterfac)
+
+    def _filter(self, q):
+        return self.filtr * q
+
+    def _do_external_forcing(self):
+        pass
+
+    def _initialize_logger(self):
+        self.logger = logging.getLogger(__name__)
+        if self.logfile is not None:
+            handler = logging.FileHandler(filename=self.logfile, mode='w')
+        else:
+            handler = logging.StreamHandler()
+        handler.setFormatter(logging.Formatter('%(levelname)s: %(message)s'))
+        if not self.logger.handlers:
+            self.logger.addHandler(handler)
+        self.logger.setLevel(self.log_level * 10)
+        self.logger.propagate = False
+        self.logger.info(' Logger initialized')
+
+    # ------------------------------------------------------------------
+    # helpers used by diagnostics and parameterizations
+    # ------------------------------------------------------------------
+    def _advect(self, q, u=None, v=None):
+        """Spectral advective tendency ik (uq)^ + il (vq)^ of real q
+        (``pyqg/model.py:539-558``); 2-D inputs give a 2-D result."""
+        u = self.u if u is None else u
+        v = self.v if v is None else v
+        uq, vq = u * q, v * q
+        flat = uq.ndim == 2
+        if flat:
+            uq, vq = uq[np.newaxis], vq[np.newaxis]
+        tend = self.ik * self.fft(np.ascontiguousarray(uq)) + \
+            self.il * self.fft(np.ascontiguousarray(vq))
+        return tend[0] if flat else tend
+
+    def _print_status(self):
+        """Log KE and CFL every `twrite` steps; fail if CFL >= 1."""
+        if self.log_level and (self.tc % self.twrite) == 0:
+            self.ke = self._calc_ke()
+            self.cfl = self._calc_cfl()
+            self.logger.info('Step: %i, Time: %3.2e, KE: %3.2e, CFL: %4.3f',
+                             self.tc, self.t, self.ke, self.cfl)
+            assert self.cfl < 1., self.logger.error('CFL condition violated')
+
+    def _calc_diagnostics(self):
+        if self._diagnostics_due(self.t, self.tc):
+            self._increment_diagnostics()
+
+    def _calc_cfl(self):
+        raise NotImplementedError('needs to be implemented by Model subclass')
+
+    def _calc_ke(self):
+        raise NotImplementedError('needs to be implemented by Model subclass')
+
+    def spec_var(self, ph):
+        """Variance of p from its half-plane Fourier coefficients."""
+        var_dens = 2. * np.abs(ph) ** 2 / self.M ** 2
+        var_dens[..., 0] = var_dens[..., 0] / 2.
+        var_dens[..., -1] = var_dens[..., -1] / 2.
+        return var_dens.sum()
+
+    # ------------------------------------------------------------------
+    # vertical structure (used by LayeredModel)
+    # ------------------------------------------------------------------
+    def vertical_modes(self):
+        """Eigen-decomposition of the stretching matrix (baroclinic modes)."""
+        evals, evecs = np.linalg.eig(-self.S)
+        order = evals.argsort()
+        self.kdi2 = evals[order]
+        self.radii = np.zeros_like(self.kdi2)
+        self.radii[0] = np.sqrt(self.g * self.H) / np.abs(self.f)
+        self.radii[1:] = 1. / np.sqrt(self.kdi2[1:])
+        self.pmodes = evecs[:, order]
+        norm = (self.H / (self.Hi[:, np.newaxis] * (self.pmodes ** 2)).sum(axis=0)) ** 0.5
+        self.pmodes = norm[np.newaxis, :] * self.pmodes
+
+    def modal_projection(self, p, forward=True):
+        """Project layer field p onto the vertical modes (or back)."""
+        if forward:
+            flat = p.reshape(p.shape[0], -1)
+            return np.linalg.solve(self.pmodes, flat).reshape(p.shape)
+        return np.einsum("ik,k...->i...", self.pmodes, p)
+
+    def subgrid_forcing(self, **kwargs):
+        raise ValueError(
+            "This method was found to be buggy and removed for now. "
+            "It will be re-added in a future release. "
+            "See https://github.com/pyqg/pyqg/pull/308 for details. ")
+
+    # ------------------------------------------------------------------
+    # diagnostics registry (pyqg/model.py:630-820)
+    # ------------------------------------------------------------------
+    def _initialize_diagnostics(self, diagnostics_list):
+        self.diagnostics = dict()
+        self._initialize_core_diagnostics()
+        self._initialize_model_diagnostics()
+        if diagnostics_list == 'all':
+            pass
+        elif diagnostics_list == 'none':
+            self.set_active_diagnostics([])
+        else:
+            self.set_active_diagnostics(diagnostics_list)
+
+    def set_active_diagnostics(self, diagnostics_list):
+        for name, d in self.diagnostics.items():
+            d['active'] = name in diagnostics_list
+
+    _set_active_diagnostics = set_active_diagnostics
+
+    def _ab_coefficients(self):
+        dt = self.dt
+        if self.ablevel == 0:
+            return dt, 0.0, 0.0
+        if self.ablevel == 1:
+            return 1.5 * dt, -0.5 * dt, 0.0
+        return 23. / 12. * dt, -16. / 12. * dt, 5. / 12. * dt
+
+    def _filter_dissipation(self):
+        """Change of qh the filter will make in the coming step."""
+        dt1, dt2, dt3 = self._ab_coefficients()
+        qh, dq, dqp, dqpp = self.qh, self.dqhdt, self.dqhdt_p, self.dqhdt_pp
+        out = np.zeros_like(qh)
+        for z in range(self.nz):
+            out[z] = (self.filtr - 1.) * (qh[z] + dt1 * dq[z] + dt2 * dqp[z] + dt3 * dqpp[z])
+        return out
+
+    def _initialize_core_diagnostics(self):
+        M2 = lambda m: m.M ** 2
+        add = self.add_diagnostic
+        add('Ensspec', description='enstrophy spectrum',
+            function=lambda m: np.abs(m.qh) ** 2 / M2(m),
+            units='s^-2', dims=('lev', 'l', 'k'))
+        add('KEspec', description='kinetic energy spectrum',
+            function=lambda m: m.wv2 * np.abs(m.ph) ** 2 / M2(m),
+            units='m^2 s^-2', dims=('lev', 'l', 'k'))
+        add('EKEdiss', description='total energy dissipation by bottom drag',
+            function=lambda m: m.Hi[-1] / m.H * m.rek * (m.v[-1] ** 2 + m.u[-1] ** 2).mean(),
+            units='m^2 s^-3', dims=('time',))
+        add('KEfrictionspec', description='total energy dissipation spectrum by bottom drag',
+            function=lambda m: -m.rek * m.Hi[-1] / m.H * m.wv2 * np.abs(m.ph[-1]) ** 2 / M2(m),
+            units='m^2 s^-3', dims=('l', 'k'))
+        add('EKE', description='mean eddy kinetic energy',
+            function=lambda m: 0.5 * (m.v ** 2 + m.u ** 2).mean(axis=-1).mean(axis=-1),
+            units='m^2 s^-2', dims=('lev',))
+        add('Dissspec', description='Spectral contribution of filter dissipation to total energy',
+            function=lambda m: -np.tensordot(m.Hi, np.conj(m.ph) * m._filter_dissipation(),
+                                             axes=(0, 0)).real / m.H / m.dt / M2(m),
+            units='m^2 s^-3', dims=('l', 'k'))
+        add('ENSDissspec', description='Spectral contribution of filter dissipation to barotropic enstrophy',
+            function=lambda m: np.tensordot(m.Hi, np.conj(m.qh) * m._filter_dissipation(),
+                                            axes=(0, 0)).real / m.H / m.dt / M2(m),
+            units='s^-3', dims=('l', 'k'))
+        add('paramspec', description='Spectral contribution of subgrid parameterization to energy (if present)',
+            function=lambda m: m._calc_parameterization_spectrum(),
+            units='m^2 s^-3', dims=('l', 'k'), skip_comparison=True)
+        add('ENSparamspec', description='Spectral contribution of subgrid parameterization to enstrophy',
+            function=lambda m: m._calc_parameterization_enstrophy_spectrum(),
+            units='s^-3', dims=('l', 'k'), skip_comparison=True)
+
+    def _calc_parameterization_contribution(self):
+        """Spectral dq/dt added by the hooks in the current step."""
+        dqh = np.zeros_like(self.qh)
+        if self.uv_parameterization is not None:
+            ik = np.broadcast_to(np.asarray(self._ik)[np.newaxis, :], self.wv2.shape)
+            il = np.broadcast_to(np.asarray(self._il)[:, np.newaxis], self.wv2.shape)
+            dqh += -il * self.duh + ik * self.dvh
+        if self.q_parameterization is not None:
+            dqh += self.dqh
+        return dqh
+
+    def _height_ratios(self):
+        return (self.Hi / self.H)[:, np.newaxis, np.newaxis]
+
+    def _calc_parameterization_spectrum(self):
+        dqh = self._calc_parameterization_contribution()
+        return -np.real((self._height_ratios() * np.conj(self.ph) * dqh).sum(axis=0)) / self.M ** 2
+
+    def _calc_parameterization_enstrophy_spectrum(self):
+        dqh = self._calc_parameterization_contribution()
+        return np.real((self._height_ratios() * np.conj(self.qh) * dqh).sum(axis=0)) / self.M ** 2
+
+    def _calc_derived_fields(self):
+        pass
+
+    def _initialize_model_diagnostics(self):
+        pass
+
+    def add_diagnostic(self, diag_name, description=None, function=None,
+                       units=None, dims=None, **kw):
+        assert hasattr(function, '__call__')
+        assert isinstance(diag_name, str)
+        entry = dict(description=description, units=units, dims=dims,
+                     active=True, count=0, function=function)
+        entry.update(**kw)
+        self.diagnostics[diag_name] = entry
+
+    def describe_diagnostics(self):
+        print('NAME               | DESCRIPTION')
+        print(80 * '-')
+        for name in sorted(self.diagnostics):
+            print('{:<10} | {:<54}'.format(name, self.diagnostics[name]['description']))
+
+    def _increment_diagnostics(self):
+        self._calc_derived_fields()
+        for name, d in self.diagnostics.items():
+            if not d['active']:
+                continue
+            value = d['function'](self)
+            if d['count'] == 0:
+                d['value'] = value
+            else:
+                d['value'] += value
+            d['count'] += 1
+
+    def get_diagnostic(self, dname):
+        d = self.diagnostics[dname]
+        if 'value' not in d:
+            raise DiagnosticNotFilledError(dname)
+        return d['value'] / d['count']
+
+    def set_qh(self, qh):
+        warnings.warn("Method deprecated. Set model.qh directly instead. ",
+                      DeprecationWarning)
+        self.qh = qh
+
+    def set_q(self, q):
+        warnings.warn("Method deprecated. Set model.q directly instead. ",
+                      DeprecationWarning)
+        self.q = q
+
+    def to_dataset(self):
+        """Convert the model state to an xarray Dataset (needs xarray)."""
+        from .xarray_output import model_to_dataset
+        return model_to_dataset(self)
+
+    @property
+    def parameterization(self):
+        if self.q_parameterization and self.uv_parameterization:
+            warnings.warn("Model has multiple parameterizations, "
+                          "but only returning PV")
+        return self.q_parameterization or self.uv_parameterization

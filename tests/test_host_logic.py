@@ -1,0 +1,168 @@
+"""CPU tests of the host side: the C ABI library loads and exports every
+symbol declared in include/*.h (no compute calls), and the model constants
+(grid, filter, inversion matrices, background) equal the reference's."""
+import glob
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO, golden
+
+
+def header_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names |= set(re.findall(r"\b(pqg_\w+)\s*\(", text))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pyqg_gb300 import _lib, build
+    if not os.path.exists(build.lib_path()):
+        build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_header_symbol(lib):
+    names = header_symbols()
+    assert len(names) >= 20
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+
+
+def test_binding_signatures_cover_header():
+    from pyqg_gb300 import _lib
+    assert header_symbols() == set(_lib.SIGNATURES)
+
+
+def test_library_reports_version_and_errors(lib):
+    assert lib.pqg_version() >= 100
+    assert lib.pqg_plan_create(None, 2, 64, 64) == 1   # PQG_ERR_INVALID, no GPU touched
+    assert b"NULL" in lib.pqg_last_error()
+
+
+def test_product_refuses_to_run_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    import pyqg_gb300 as P
+    with pytest.raises(RuntimeError, match="CUDA"):
+        P.QGModel()
+
+
+def _qg_consts(n, L=1e6, rd=15000.0, delta=0.25, beta=1.5e-11, U1=0.025,
+               U2=0.0, filterfac=23.6):
+    from pyqg_gb300.model import grid_constants, spectral_filter
+    from pyqg_gb300.qg_model import qg_inversion_matrix
+    g = grid_constants(n, n, L, L)
+    F1 = rd ** -2 / (1. + delta)
+    F2 = delta * F1
+    return dict(a=qg_inversion_matrix(g["wv2"], F1, F2), kk=g["kk"], ll=g["ll"],
+                filtr=spectral_filter(g["k"], g["l"], g["dx"], g["dy"], filterfac),
+                Qy=np.array([beta + F1 * (U1 - U2), beta - F2 * (U1 - U2)]))
+
+
+def test_qg_constants_equal_reference():
+    g = golden("qg_c1_nx64.npz")
+    c = _qg_consts(64)
+    for k in ("a", "kk", "ll", "filtr", "Qy"):
+        np.testing.assert_array_equal(c[k], g[k], err_msg=k)
+
+
+def test_layered_constants_equal_reference():
+    from pyqg_gb300.model import grid_constants, spectral_filter
+    from pyqg_gb300.layered_model import stretching_matrix, layered_inversion_matrix
+    g = golden("layered_nz3_nx32.npz")
+    grid = grid_constants(32, 32, 1e6, 1e6)
+    rho = np.arange(3) * 0.3 + 1025
+    gpi = 9.81 * (rho[1:] - rho[:-1]) / rho[:-1]
+    f = 0.0001236812857687059
+    S = stretching_matrix(3, f ** 2, np.array([500., 1000., 2500.]), gpi)
+    a = layered_inversion_matrix(S, grid["wv2"])
+    np.testing.assert_allclose(a, g["a"], rtol=1e-15, atol=0)
+    Qy = 1.5e-11 - S @ np.array([0.05, 0.02, 0.0])
+    np.testing.assert_allclose(Qy, g["Qy"], rtol=1e-15)
+    np.testing.assert_array_equal(
+        spectral_filter(grid["k"], grid["l"], grid["dx"], grid["dy"], 23.6), g["filtr"])
+
+
+def test_layered_fixture_params_constants():
+    """The reference's own LayeredModel test fixture parameters (nx=64)."""
+    from pyqg_gb300.model import grid_constants
+    from pyqg_gb300.layered_model import stretching_matrix, layered_inversion_matrix
+    g = golden("layered_fixture_nx64.npz")
+    p = json.loads(str(g["params_json"]))
+    grid = grid_constants(64, 64, p["L"], p["L"])
+    rho = np.array(p["rho"])
+    gpi = p["g"] * (rho[1:] - rho[:-1]) / rho[:-1]
+    S = stretching_matrix(3, p["f"] ** 2, np.array(p["H"], dtype=float), gpi)
+    np.testing.assert_allclose(layered_inversion_matrix(S, grid["wv2"]), g["a"],
+                               rtol=1e-14, atol=0)
+
+
+def test_stretching_matrix_properties():
+    """S has zero row sums and H S is symmetric (pyqg/tests/test_layered.py)."""
+    from pyqg_gb300.layered_model import stretching_matrix
+    Hi = np.array([.1, .1, .3])
+    rho = np.array([.1, .3, .5])
+    gpi = 9.81 * (rho[1:] - rho[:-1]) / rho[:-1]
+    S = stretching_matrix(3, 1.0, Hi, gpi)
+    assert np.all(S.sum(axis=1) == 0.)
+    HS = np.diag(Hi) @ S
+    np.testing.assert_allclose(HS, HS.T, atol=1e-16)
+
+
+def test_single_layer_inversions():
+    from pyqg_gb300.model import grid_constants
+    for case in ("bt_nx32.npz", "sqg_nx32.npz"):
+        g = golden(case)
+        grid = grid_constants(32, 32, 2 * np.pi, 2 * np.pi)
+        if case.startswith("bt"):
+            a = -grid["wv2i"][np.newaxis, np.newaxis]
+        else:
+            a = np.sqrt(grid["wv2i"])[np.newaxis, np.newaxis]
+        np.testing.assert_array_equal(a, g["a"])
+
+
+def test_parameterization_algebra():
+    import pyqg_gb300 as P
+    smag, zb = P.Smagorinsky(), P.ZannaBolton2020()
+    comb = 0.5 * smag + 0.75 * zb
+    assert comb.parameterization_type == "uv_parameterization"
+    with pytest.raises(AssertionError):
+        P.BackscatterBiharmonic() + smag
+
+
+class _FakeModel:
+    """Host-side stand-in with the attributes the batching logic reads."""
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def test_fused_run_length_stops_at_observation_points():
+    from pyqg_gb300.model import Model
+    m = _FakeModel(t=0.0, tc=0, dt=10.0, tmax=1e9, tavestart=1e30, taveints=1.0,
+                   log_level=1, twrite=25, q_parameterization=None,
+                   uv_parameterization=None)
+    m._fusable = lambda: True
+    m._diagnostics_due = lambda t, tc: Model._diagnostics_due(m, t, tc)
+    m._status_due = lambda tc: Model._status_due(m, tc)
+    # status every 25 steps: the first batch ends after step 25
+    assert Model._fusable_run_length(m) == 25
+    m.tc, m.t = 25, 250.0
+    assert Model._fusable_run_length(m) == 25
+    # tmax cuts the batch
+    m.tmax = 300.0
+    assert Model._fusable_run_length(m) == 5
+    # diagnostics due now: no fused step
+    m.tmax, m.tavestart = 1e9, 0.0
+    assert Model._fusable_run_length(m) == 0
+    # a snapshot predicate ends the batch after the matching step
+    m.tavestart, m.log_level = 1e30, 0
+    assert Model._fusable_run_length(m, lambda t, tc: tc % 7 == 0) == 3
