@@ -150,7 +150,8 @@ def test_model_families_vs_reference(P, quiet, case):
     else:
         m = P.SQGModel(L=2. * np.pi, nx=32, beta=0., H=1., dt=0.0025, **quiet)
     np.testing.assert_allclose(m.a.real, g["a"], rtol=1e-15, atol=0)
-    np.testing.assert_array_equal(m.filtr, g["filtr"])
+    # libm exp may differ by an ulp between the x86 reference host and here
+    np.testing.assert_allclose(m.filtr, g["filtr"], rtol=1e-14, atol=0)
     m.q = g["q0"]
     m._step_forward()
     assert rel_l2(m.q, g["q_1"]) < TOL_STAGE
