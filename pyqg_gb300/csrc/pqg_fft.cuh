@@ -147,6 +147,8 @@ template <bool INV> struct Dft<8, INV> {
 // Butterflies a thread keeps in registers per stage for radix R: the block
 // must satisfy blockDim.x * MaxIt<R> >= n / R for every stage.
 template <int R> struct MaxIt { static constexpr int value = R == 2 ? 4 : (R == 8 || R == 5 ? 1 : 2); };
+// (blockDim >= n / 8 covers radix 2, 4 and 8 stages; radix 3 needs n / 6,
+// radix 5 needs n / 5)
 
 // One Stockham stage (radix R, Ns = product of earlier radices) on `nseq`
 // sequences of length n at buf + s*stride, in place through registers.
@@ -220,6 +222,52 @@ __device__ void fft_run(double2* buf, int stride, int nseq, const FftDesc& d,
 }
 
 // ---------------------------------------------------------------------------
+// Compile-time plans for power-of-two lengths n = 2^a: radix 8 stages, then
+// radix 4 (two instead of a final 8*2), then a radix 2 only for n = 2, 8*2...
+// The host-side factorisation produces the same radix order, so the runtime
+// and compile-time paths run the same stages and give identical results.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int pow2_eights(int a) { return (a % 3 == 1 && a >= 4) ? a / 3 - 1 : a / 3; }
+__host__ __device__ constexpr int pow2_fours(int a) { return (a % 3 == 1) ? (a >= 4 ? 2 : 0) : (a % 3 == 2 ? 1 : 0); }
+__host__ __device__ constexpr int pow2_radix(int a, int s) {
+  // radix of the stage that starts at Ns = 2^s
+  return s < 3 * pow2_eights(a) ? 8 : (s < 3 * pow2_eights(a) + 2 * pow2_fours(a) ? 4 : 2);
+}
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+
+template <int N, int NS, bool INV>
+struct Pow2Fft {
+  static constexpr int R = pow2_radix(ilog2(N), ilog2(NS));
+  static __device__ __forceinline__ void run(double2* buf, int stride, int nseq,
+                                             const double2* __restrict__ tw, int twstep) {
+    fft_stage<R, INV>(buf, stride, nseq, N, NS, tw, twstep);
+    Pow2Fft<N, NS * R, INV>::run(buf, stride, nseq, tw, twstep);
+  }
+};
+template <int N, bool INV>
+struct Pow2Fft<N, N, INV> {
+  static __device__ __forceinline__ void run(double2*, int, int, const double2*, int) {}
+};
+
+// FFT engines used as kernel template arguments: a runtime mixed-radix plan,
+// or a compile-time power-of-two plan of length 2^LOGN.
+struct FftRuntime {
+  template <bool INV>
+  static __device__ __forceinline__ void run(double2* buf, int stride, int nseq, const FftDesc& d,
+                                             const double2* __restrict__ tw, int twstep) {
+    fft_run<INV>(buf, stride, nseq, d, tw, twstep);
+  }
+};
+template <int LOGN>
+struct FftPow2 {
+  template <bool INV>
+  static __device__ __forceinline__ void run(double2* buf, int stride, int nseq, const FftDesc&,
+                                             const double2* __restrict__ tw, int twstep) {
+    Pow2Fft<(1 << LOGN), 1, INV>::run(buf, stride, nseq, tw, twstep);
+  }
+};
+
+// ---------------------------------------------------------------------------
 // real <-> half-length complex packing for the row transforms (length N = 2M)
 // tw is the length-N table exp(-2 pi i m / N).
 // ---------------------------------------------------------------------------
@@ -267,16 +315,15 @@ __device__ __forceinline__ void r2c_post(const double2* z,
 }
 
 // ---------------------------------------------------------------------------
-// pointwise physics, written to reproduce the reference's C arithmetic
-// (no contraction; complex products with purely real / imaginary factors
-// reduce to the real products below).
+// pointwise physics (reference expressions, evaluated with fused
+// multiply-adds; complex products with purely real / imaginary factors
+// reduce to the real products below)
 // ---------------------------------------------------------------------------
 
 // ph = sum_{z'} a[z, z'] qh[z'] accumulated from zero in z' order
 // (pyqg/kernel.pyx:323-338).
 __device__ __forceinline__ double2 ph_acc(double2 acc, double a, double2 qh) {
-  return make_double2(__dadd_rn(acc.x, __dmul_rn(a, qh.x)),
-                      __dadd_rn(acc.y, __dmul_rn(a, qh.y)));
+  return make_double2(__fma_rn(a, qh.x, acc.x), __fma_rn(a, qh.y, acc.y));
 }
 // uh = -il ph (pyqg/kernel.pyx:346)
 __device__ __forceinline__ double2 uh_of(double l, double2 ph) {
@@ -290,35 +337,28 @@ __device__ __forceinline__ double2 vh_of(double k, double2 ph) {
 __device__ __forceinline__ double2 tendency(double k, double l, double kQy,
                                             double2 uqh, double2 vqh,
                                             double2 ph) {
-  const double re = __dadd_rn(__dadd_rn(__dmul_rn(k, uqh.y), __dmul_rn(l, vqh.y)),
-                              __dmul_rn(kQy, ph.y));
-  const double im = __dadd_rn(__dadd_rn(__dmul_rn(k, uqh.x), __dmul_rn(l, vqh.x)),
-                              __dmul_rn(kQy, ph.x));
+  const double re = __fma_rn(kQy, ph.y, __fma_rn(l, vqh.y, __dmul_rn(k, uqh.y)));
+  const double im = __fma_rn(kQy, ph.x, __fma_rn(l, vqh.x, __dmul_rn(k, uqh.x)));
   return make_double2(re, -im);
 }
 // dqhdt += (rek k2l2) ph (pyqg/kernel.pyx:456-460)
 __device__ __forceinline__ double2 friction(double2 dq, double rk2, double2 ph) {
-  return make_double2(__dadd_rn(dq.x, __dmul_rn(rk2, ph.x)),
-                      __dadd_rn(dq.y, __dmul_rn(rk2, ph.y)));
+  return make_double2(__fma_rn(rk2, ph.x, dq.x), __fma_rn(rk2, ph.y, dq.y));
 }
 // dqhdt += -il duh + ik dvh (pyqg/kernel.pyx:417-421)
 __device__ __forceinline__ double2 uv_curl_add(double2 dq, double k, double l,
                                                double2 duh, double2 dvh) {
   // -il duh = (l duh.y, -l duh.x); ik dvh = (-k dvh.y, k dvh.x)
-  const double re = __dadd_rn(__dmul_rn(l, duh.y), -__dmul_rn(k, dvh.y));
-  const double im = __dadd_rn(-__dmul_rn(l, duh.x), __dmul_rn(k, dvh.x));
+  const double re = __fma_rn(-k, dvh.y, __dmul_rn(l, duh.y));
+  const double im = __fma_rn(k, dvh.x, -__dmul_rn(l, duh.x));
   return make_double2(__dadd_rn(dq.x, re), __dadd_rn(dq.y, im));
 }
 // qh_new = filtr (qh + c1 dq + c2 dq_p + c3 dq_pp) (pyqg/kernel.pyx:502-507)
 __device__ __forceinline__ double2 ab_update(double f, double2 qh, double2 dq,
                                              double2 dqp, double2 dqpp,
                                              double c1, double c2, double c3) {
-  const double re = __dadd_rn(__dadd_rn(__dadd_rn(qh.x, __dmul_rn(c1, dq.x)),
-                                        __dmul_rn(c2, dqp.x)),
-                              __dmul_rn(c3, dqpp.x));
-  const double im = __dadd_rn(__dadd_rn(__dadd_rn(qh.y, __dmul_rn(c1, dq.y)),
-                                        __dmul_rn(c2, dqp.y)),
-                              __dmul_rn(c3, dqpp.y));
+  const double re = __fma_rn(c3, dqpp.x, __fma_rn(c2, dqp.x, __fma_rn(c1, dq.x, qh.x)));
+  const double im = __fma_rn(c3, dqpp.y, __fma_rn(c2, dqp.y, __fma_rn(c1, dq.y, qh.y)));
   return make_double2(__dmul_rn(f, re), __dmul_rn(f, im));
 }
 

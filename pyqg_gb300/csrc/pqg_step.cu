@@ -100,6 +100,7 @@ struct RowAdvArgs {
   int rb;
 };
 
+template <class FX>
 __global__ void k_row_adv(Geo g, RowAdvArgs A) {
   extern __shared__ double2 sm[];
   const int M = g.M, nk = g.nk, nx = g.nx;
@@ -138,7 +139,7 @@ __global__ void k_row_adv(Geo g, RowAdvArgs A) {
   // Buffers of a field hold A.rb rows; rows past `rb` (last CTA) are unused.
   {
     const int nmix = (A.mixU ? 1 : 0) + (A.mixV ? 1 : 0) + (A.mixQ ? 1 : 0);
-    if (nmix) fft_run<true>(bU, M, nmix * A.rb, g.fx, tw, 2);
+    if (nmix) FX::template run<true>(bU, M, nmix * A.rb, g.fx, tw, 2);
   }
 
   // -- unpack, products, optional stores -------------------------------------
@@ -168,7 +169,7 @@ __global__ void k_row_adv(Geo g, RowAdvArgs A) {
   __syncthreads();
 
   // -- forward transforms of uq, vq and R2C post-processing -------------------
-  fft_run<false>(bU, M, 2 * A.rb, g.fx, tw, 2);
+  FX::template run<false>(bU, M, 2 * A.rb, g.fx, tw, 2);
   for (int t = threadIdx.x; t < 2 * rb * half; t += blockDim.x) {
     const int f = t / (rb * half);
     const int rem = t - f * rb * half;
@@ -402,6 +403,7 @@ struct FusedColArgs {
   double c1, c2, c3;
 };
 
+template <class FY>
 __global__ void k_col_fused(Geo g, Consts c, FusedColArgs A) {
   extern __shared__ double2 sm[];
   cg::cluster_group cluster = cg::this_cluster();
@@ -420,7 +422,7 @@ __global__ void k_col_fused(Geo g, Consts c, FusedColArgs A) {
     bQO[l] = A.qh[o];
   }
   __syncthreads();
-  fft_run<false>(bU, ny, 2, g.fy, tw, 1);
+  FY::template run<false>(bU, ny, 2, g.fy, tw, 1);
   cluster.sync();  // qh(old) of every layer is in shared memory
 
   const double kk = c.kk[k], kQy = c.kQy[z * nk + k];
@@ -460,7 +462,7 @@ __global__ void k_col_fused(Geo g, Consts c, FusedColArgs A) {
     bV[l] = vh_of(kk, p);
   }
   cluster.sync();  // remote reads of bQN done before it is transformed
-  fft_run<true>(bU, ny, 3, g.fy, tw, 1);  // U, V, qh(new): contiguous
+  FY::template run<true>(bU, ny, 3, g.fy, tw, 1);  // U, V, qh(new): contiguous
   for (int l = threadIdx.x; l < ny; l += blockDim.x) {
     const size_t o = cidx(z, l, k, ny, nk);
     A.mixU[o] = bU[l];
@@ -509,9 +511,19 @@ static bool factor(int n, FftDesc& d) {
   d.code = 0;
   int m = n;
   auto push = [&](int r) { d.code |= (unsigned long long)r << (4 * d.nst); d.nst++; m /= r; };
-  // radix-4 first, then 2, 3, 5 (radix order only affects rounding)
-  while (m % 4 == 0 && d.nst < kMaxStages) push(4);
-  while (m % 2 == 0 && d.nst < kMaxStages) push(2);
+  // power-of-two part: radix 8 where possible, radix 4 instead of a final
+  // radix 2 (radix 2 costs more FP64 operations per point), then 3 and 5
+  int a = 0;
+  while (m % 2 == 0) { m /= 2; a++; }
+  m = n;
+  int eights = pow2_eights(a), fours = pow2_fours(a);
+  int twos = a - 3 * eights - 2 * fours;
+  if (const char* e = getenv("PQG_RADIX4")) {  // tuning: radix 4/2 only
+    if (e[0] == '1') { eights = 0; fours = a / 2; twos = a % 2; }
+  }
+  for (int i = 0; i < eights && d.nst < kMaxStages; i++) push(8);
+  for (int i = 0; i < fours && d.nst < kMaxStages; i++) push(4);
+  for (int i = 0; i < twos && d.nst < kMaxStages; i++) push(2);
   while (m % 3 == 0 && d.nst < kMaxStages) push(3);
   while (m % 5 == 0 && d.nst < kMaxStages) push(5);
   return m == 1;
@@ -604,6 +616,47 @@ static const double2* dc(const double* x) { return reinterpret_cast<const double
 #define CHECK_LAUNCH() PQG_CUDA(cudaGetLastError())
 
 // ---------------------------------------------------------------------------
+// kernel selection: compile-time power-of-two plans for the hot kernels
+// ---------------------------------------------------------------------------
+typedef void (*RowAdvFn)(Geo, RowAdvArgs);
+typedef void (*ColFusedFn)(Geo, Consts, FusedColArgs);
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static RowAdvFn row_adv_kernel(int M) {
+  if (is_pow2(M) && !getenv("PQG_GENERIC_FFT")) {
+    switch (ilog2(M)) {
+      case 3: return k_row_adv<FftPow2<3>>;
+      case 4: return k_row_adv<FftPow2<4>>;
+      case 5: return k_row_adv<FftPow2<5>>;
+      case 6: return k_row_adv<FftPow2<6>>;
+      case 7: return k_row_adv<FftPow2<7>>;
+      case 8: return k_row_adv<FftPow2<8>>;
+      case 9: return k_row_adv<FftPow2<9>>;
+      case 10: return k_row_adv<FftPow2<10>>;
+      default: break;
+    }
+  }
+  return k_row_adv<FftRuntime>;
+}
+
+static ColFusedFn col_fused_kernel(int ny) {
+  if (is_pow2(ny) && !getenv("PQG_GENERIC_FFT")) {
+    switch (ilog2(ny)) {
+      case 4: return k_col_fused<FftPow2<4>>;
+      case 5: return k_col_fused<FftPow2<5>>;
+      case 6: return k_col_fused<FftPow2<6>>;
+      case 7: return k_col_fused<FftPow2<7>>;
+      case 8: return k_col_fused<FftPow2<8>>;
+      case 9: return k_col_fused<FftPow2<9>>;
+      case 10: return k_col_fused<FftPow2<10>>;
+      default: break;
+    }
+  }
+  return k_col_fused<FftRuntime>;
+}
+
+// ---------------------------------------------------------------------------
 // launch helpers (stage kernels)
 // ---------------------------------------------------------------------------
 static int launch_row_adv(pqg_plan* p, const RowAdvArgs& A0, cudaStream_t st) {
@@ -612,7 +665,7 @@ static int launch_row_adv(pqg_plan* p, const RowAdvArgs& A0, cudaStream_t st) {
   A.Ubg = p->Ubg;
   const int nrows = p->nz * p->ny;
   const int grid = (nrows + A.rb - 1) / A.rb;
-  k_row_adv<<<grid, p->T_row, row_adv_smem(p, A.rb), st>>>(geo(p), A);
+  row_adv_kernel(p->M)<<<grid, p->T_row, row_adv_smem(p, A.rb), st>>>(geo(p), A);
   CHECK_LAUNCH();
   return PQG_OK;
 }
@@ -662,7 +715,7 @@ static int launch_col_fused(pqg_plan* p, const FusedColArgs& A, cudaStream_t st)
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  PQG_CUDA(cudaLaunchKernelEx(&cfg, k_col_fused, geo(p), consts(p), A));
+  PQG_CUDA(cudaLaunchKernelEx(&cfg, col_fused_kernel(p->ny), geo(p), consts(p), A));
   return PQG_OK;
 }
 
@@ -677,7 +730,9 @@ static int set_smem_limits() {
   static bool done = false;
   if (done) return PQG_OK;
   const int big = 200 * 1024;
-  PQG_CUDA(cudaFuncSetAttribute(k_row_adv, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  for (int m = 8; m <= 1024; m *= 2)
+    PQG_CUDA(cudaFuncSetAttribute(row_adv_kernel(m), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(row_adv_kernel(3), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(k_row_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(k_col_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -685,8 +740,12 @@ static int set_smem_limits() {
   PQG_CUDA(cudaFuncSetAttribute(k_col_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(k_col_adv, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(k_col_ab3, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PQG_CUDA(cudaFuncSetAttribute(k_col_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PQG_CUDA(cudaFuncSetAttribute(k_col_fused, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  for (int n = 16; n <= 1024; n *= 2) {
+    PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(n), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  }
+  PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(3), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(3), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   done = true;
   return PQG_OK;
 }
@@ -727,7 +786,12 @@ PQG_API int pqg_plan_create(pqg_plan** out, int nz, int ny, int nx) {
   p->rb = std::max(1, std::min(4, 128 / p->M));
   p->T_row_batch = p->T_row;
   p->rb_batch = std::max(1, std::min(8, 256 / p->M));
-  if (p->T_col < min_threads(p->fy) || p->T_row < min_threads(p->fx)) {
+  // tuning overrides (block shapes only; results do not depend on them)
+  if (const char* e = getenv("PQG_T_ROW")) p->T_row = atoi(e);
+  if (const char* e = getenv("PQG_RB")) p->rb = atoi(e);
+  if (const char* e = getenv("PQG_T_COL")) p->T_col = atoi(e);
+  if (p->T_col < min_threads(p->fy) || p->T_row < min_threads(p->fx) || p->rb < 1 ||
+      p->T_row > 1024 || p->T_col > 1024) {
     delete p;
     return fail(PQG_ERR_UNSUPPORTED, "transform too long for the block size");
   }
