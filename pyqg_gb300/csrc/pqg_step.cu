@@ -779,7 +779,7 @@ PQG_API int pqg_plan_create(pqg_plan** out, int nz, int ny, int nx) {
     return fail(PQG_ERR_UNSUPPORTED, "grid too large for the shared-memory kernels");
   }
   // block shapes: the Stockham stages need blockDim * MaxIt >= n / R
-  p->T_col = std::max(64, std::min(256, ny / 2));
+  p->T_col = std::max(64, std::min(256, ny));
   p->T_row = std::max(64, std::min(256, p->M));
   if (p->T_col < min_threads(p->fy)) p->T_col = std::min(1024, (min_threads(p->fy) + 31) / 32 * 32);
   if (p->T_row < min_threads(p->fx)) p->T_row = std::min(1024, (min_threads(p->fx) + 31) / 32 * 32);
