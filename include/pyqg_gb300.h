@@ -156,6 +156,25 @@ int pqg_step(pqg_plan *plan, pqg_state *state, int nsteps,
 int pqg_step_profile(pqg_plan *plan, pqg_state *state, int nsteps,
                      double *ms, int *counts, void *stream);
 
+/* Forward 2-D real transform for callers that cannot allocate device
+ * memory (no counterpart in the reference).  Same result as pqg_rfft2, but
+ * needs no plan: the transposition scratch and twiddle tables are static
+ * device arrays of the library (about 8.1 MiB per device, kept until the
+ * process exits).  Intended for code whose device memory belongs to another
+ * allocator (a framework's caching allocator or a fixed arena) and for code
+ * that must not stall the device, as cudaMalloc / cudaFree can.
+ *   - nplanes * ny * (nx/2 + 1) must not exceed PQG_NOALLOC_MAX_COMPLEX;
+ *     larger requests fail with PQG_ERR_UNSUPPORTED and a message.
+ *   - The first call on a device looks up the arrays' device addresses and
+ *     a call whose (ny, nx) differs from the previous call's on that device
+ *     uploads twiddle tables; make such calls before any stream capture.
+ *   - All calls on a device share the arrays: calls that can overlap on the
+ *     GPU (different streams without ordering) race.  Calls on one stream
+ *     are safe; no state carries over between calls. */
+#define PQG_NOALLOC_MAX_COMPLEX (1 << 19)
+int pqg_rfft2_noalloc(const double *x, double *xh, int nplanes, int ny,
+                      int nx, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,7 @@ SIGNATURES = {
                       _P]),
     "pqg_step_profile": (_I, [_P, ctypes.POINTER(State), _I,
                               ctypes.POINTER(_D), ctypes.POINTER(_I), _P]),
+    "pqg_rfft2_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
 }
 
 _lock = threading.Lock()

@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1186,6 +1187,109 @@ PQG_API int pqg_step_profile(pqg_plan* p, pqg_state* s, int nsteps, double* ms, 
     counts[0] = counts[1] = nsteps;
   }
   for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Forward 2-D real transform that allocates no device memory.
+//
+// For callers that cannot call cudaMalloc: processes whose device memory is
+// owned by another allocator (a framework's caching allocator, or a fixed
+// arena reserved at start-up), and callers that must not stall the device,
+// since cudaMalloc / cudaFree may wait for outstanding GPU work.  The
+// transposition scratch and the twiddle tables live in file-scope
+// `static __device__` arrays that every GPU loading this library keeps until
+// the process exits (about 8.1 MiB per device).  Their device addresses are
+// looked up once per device with cudaGetSymbolAddress (the first call on a
+// device, which should therefore come before any stream capture).  The
+// twiddle tables are uploaded when the (ny, nx) of a call differs from the
+// previous call's on that device; such a call is not capturable either.
+// All calls on a device share these arrays and overwrite them, so calls
+// that may overlap on the GPU (different streams, no ordering) race; calls
+// on one stream are ordered.  Every scratch element a call reads is first
+// written by that call, so nothing has to be cleared between calls.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double2 g_noalloc_scratch[PQG_NOALLOC_MAX_COMPLEX];
+static __device__ __align__(256) double2 g_noalloc_twx[2 * 2048];
+static __device__ __align__(256) double2 g_noalloc_twy[2048];
+
+namespace {
+constexpr int kMaxDevices = 64;
+struct NoAllocDevice {
+  bool ready = false;
+  double2* scratch = nullptr;
+  double2* twx = nullptr;
+  double2* twy = nullptr;
+  int tw_nx = 0, tw_ny = 0;
+};
+NoAllocDevice g_noalloc_dev[kMaxDevices];
+std::mutex g_noalloc_mutex;
+double2 g_noalloc_host_tw[2 * 2048];  // host staging for table uploads
+
+void twiddles_into(int n, double2* w) {
+  std::vector<double2> tmp;  // host memory only
+  twiddles(n, tmp);
+  std::memcpy(w, tmp.data(), sizeof(double2) * n);
+}
+}  // namespace
+
+PQG_API int pqg_rfft2_noalloc(const double* x, double* xh, int nplanes, int ny, int nx, void* stream) {
+  if (!x || !xh || nplanes < 1 || ny < 2 || nx < 2) return fail(PQG_ERR_INVALID, "bad argument to pqg_rfft2_noalloc");
+  if (nx % 2 || ny % 2) return fail(PQG_ERR_UNSUPPORTED, "nx and ny must be even");
+  if (nx / 2 > 2048 || ny > 2048) return fail(PQG_ERR_UNSUPPORTED, "nx/2 and ny must be <= 2048");
+  const long long need = (long long)nplanes * ny * (nx / 2 + 1);
+  if (need > PQG_NOALLOC_MAX_COMPLEX)
+    return fail(PQG_ERR_UNSUPPORTED, "pqg_rfft2_noalloc: nplanes*ny*(nx/2+1) = " + std::to_string(need) +
+                                         " exceeds the static scratch of " +
+                                         std::to_string(PQG_NOALLOC_MAX_COMPLEX) + " complex values");
+  pqg_plan p;  // shapes and block sizes only; no device memory
+  p.nz = 1; p.ny = ny; p.nx = nx; p.nk = nx / 2 + 1; p.M = nx / 2;
+  if (!factor(p.M, p.fx) || !factor(ny, p.fy)) return fail(PQG_ERR_UNSUPPORTED, "nx/2 and ny must factor into 2, 3 and 5");
+  p.T_col = std::max(64, std::min(256, ny / 2));
+  p.T_row = std::max(64, std::min(256, p.M));
+  if (p.T_col < min_threads(p.fy)) p.T_col = std::min(1024, (min_threads(p.fy) + 31) / 32 * 32);
+  if (p.T_row < min_threads(p.fx)) p.T_row = std::min(1024, (min_threads(p.fx) + 31) / 32 * 32);
+  p.T_row_batch = p.T_row;
+  p.rb_batch = std::max(1, std::min(8, 256 / p.M));
+  if (p.T_col < min_threads(p.fy) || p.T_row < min_threads(p.fx))
+    return fail(PQG_ERR_UNSUPPORTED, "transform too long for the block size");
+  int rc = set_smem_limits();
+  if (rc) return rc;
+  int dev = 0;
+  PQG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(PQG_ERR_UNSUPPORTED, "device ordinal out of range");
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoAllocDevice& d = g_noalloc_dev[dev];
+    if (!d.ready) {
+      // once per device, with that device current: host-side names of the
+      // arrays are not device addresses; ask the runtime for those
+      PQG_CUDA(cudaGetSymbolAddress((void**)&d.scratch, g_noalloc_scratch));
+      PQG_CUDA(cudaGetSymbolAddress((void**)&d.twx, g_noalloc_twx));
+      PQG_CUDA(cudaGetSymbolAddress((void**)&d.twy, g_noalloc_twy));
+      d.ready = true;
+    }
+    if (d.tw_nx != nx) {
+      twiddles_into(nx, g_noalloc_host_tw);
+      PQG_CUDA(cudaMemcpyAsync(d.twx, g_noalloc_host_tw, sizeof(double2) * nx, cudaMemcpyHostToDevice, st));
+      PQG_CUDA(cudaStreamSynchronize(st));
+      d.tw_nx = nx;
+    }
+    if (d.tw_ny != ny) {
+      twiddles_into(ny, g_noalloc_host_tw);
+      PQG_CUDA(cudaMemcpyAsync(d.twy, g_noalloc_host_tw, sizeof(double2) * ny, cudaMemcpyHostToDevice, st));
+      PQG_CUDA(cudaStreamSynchronize(st));
+      d.tw_ny = ny;
+    }
+    p.twx = d.twx;
+    p.twy = d.twy;
+    p.scratch = d.scratch;
+  }
+  rc = launch_row_r2c(&p, x, p.scratch, nplanes, st);
+  if (!rc) rc = launch_col_batch<false>(&p, p.scratch, reinterpret_cast<double2*>(xh), nplanes, st);
+  p.twx = p.twy = nullptr;  // not owned: keep the plan destructor-free path
+  p.scratch = nullptr;
   return rc;
 }
 
