@@ -49,50 +49,72 @@ def peaks():
 # clocks sampled during the timed region
 # --------------------------------------------------------------------------
 class ClockSampler:
+    """Streams `nvidia-smi -lms 50` for one GPU; summary() keeps the samples
+    taken between mark_start() and mark_stop()."""
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, index):
         self.index = index
         self.samples = []
-        self._stop = threading.Event()
-        self._t = None
+        self.t0 = self.t1 = None
+        self.proc = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(
-                    ["nvidia-smi", "-i", str(self.index),
-                     "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits"],
-                    capture_output=True, text=True, timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.strip().split(",")]
+            if len(parts) >= 6:
+                self.samples.append((time.time(), parts))
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+            t_end = time.time() + 5.0
+            while not self.samples and time.time() < t_end:
+                time.sleep(0.05)
+        except Exception:
+            self.proc = None
         return self
 
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_stop(self):
+        self.t1 = time.time()
+        time.sleep(0.12)   # let the sample covering the end arrive
+
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
 
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4)
-                          if len(s) > 2 + i and s[2 + i].lower() == "active"})
+        inside = [p for t, p in self.samples if self.t0 is not None and self.t0 - 0.05 <= t <= self.t1 + 0.06]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [v for v in (num(p[0]) for p in inside) if v is not None]
+        mx = [v for v in (num(p[1]) for p in inside) if v is not None]
+        reasons = sorted({self.NAMES[i] for p in inside for i in range(4)
+                          if p[2 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.samples)}
+                "samples": len(inside)}
 
 
 # --------------------------------------------------------------------------
@@ -158,23 +180,24 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     dt = 3600.0
-    secs, kind, cores = cpu_model_steps(args.warmup)  # warm-up steps
+    sample = min(args.chunk, 100)   # model steps per timed step on the CPU
+    secs, kind, cores = cpu_model_steps(max(1, args.warmup))  # warm-up steps
     times = []
     for _ in range(args.steps):
-        s, kind, cores = cpu_model_steps(args.chunk, dt=dt)
+        s, kind, cores = cpu_model_steps(sample, dt=dt)
         times.append(s)
     total = sum(times)
-    value = sim_yr_per_hr(args.steps * args.chunk, dt, total)
+    value = sim_yr_per_hr(args.steps * sample, dt, total)
     line = {"metric": METRIC, "value": value, "unit": "sim-yr/hr", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (config-2 physics), "
-                                   "%d model steps per timed step" % args.chunk,
-                       "model_steps_per_step": args.chunk, "l2": "n/a (CPU)"},
+                                   "%d model steps per timed step" % sample,
+                       "model_steps_per_step": sample, "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": value, "unit": "sim-yr/hr", "cores": cores, "kind": kind,
-                             "sample": "%d x %d config-2 steps" % (args.steps, args.chunk)},
+                             "sample": "%d x %d config-2 steps" % (args.steps, sample)},
             "e2e": {"value": value, "unit": "sim-yr/hr", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
@@ -226,25 +249,45 @@ def run_ours(args, rank, world, local_rank):
                               ctypes.c_void_p(stream.cuda_stream)))
         commit(st)
 
+    def timed(nsteps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(nsteps)]
+        for i in range(nsteps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            device_step()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    # the other transform engine, measured beside the default one
+    other = "fp64" if m.engine == "fixed" else "fixed"
+    engine = m.engine
+    alt = None
+    try:
+        m.engine = other
+        for _ in range(args.warmup):
+            device_step()
+        torch.cuda.synchronize()
+        alt_ms = timed(max(3, args.steps // 4))
+        alt = sim_yr_per_hr(len(alt_ms) * args.chunk, dt, sum(alt_ms) / 1e3)
+    except Exception:
+        alt = None
+    m.engine = engine
+
     # warm-up (also captures and caches the CUDA graphs)
     for _ in range(args.warmup):
         device_step()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     with ClockSampler(local_rank) as clocks:
         torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.zero_()
-            ev[i][0].record(stream)
-            device_step()
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
+        clocks.mark_start()
+        ms = timed(args.steps)
+        clocks.mark_stop()
     if world > 1:
         torch.distributed.barrier()
-    ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(ms) / 1e3
     if world > 1:
         t = torch.tensor([total_s], device=dev)
@@ -291,10 +334,11 @@ def run_ours(args, rank, world, local_rank):
     # row kernel: physical q 16 P)
     S = nz * nx * (nx // 2 + 1)
     Pn = nz * nx * nx
+    sfx = "_fx" if engine == "fixed" else ""
     if col_ms >= row_ms:
-        name, kms_, nbytes = "k_col_fused", col_ms, 80 * S
+        name, kms_, nbytes = "k_col_fused" + sfx, col_ms, 80 * S
     else:
-        name, kms_, nbytes = "k_row_adv", row_ms, 16 * Pn
+        name, kms_, nbytes = "k_row_adv" + sfx, row_ms, 16 * Pn
     achieved = nbytes / (kms_ * 1e-3) / 1e9
     traffic = None
     tf = os.path.join(HERE, "profiles", "traffic.json")
@@ -309,9 +353,13 @@ def run_ours(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": "sim-yr/hr", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded 1e-7 N(0,1) initial PV)",
+        "dtype": "f64" if engine == "fp64" else "f64+int64",
+        "data": "synthetic (seeded 1e-7 N(0,1) initial PV)",
         "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (config-2 physics), "
                                "%d model steps per timed step" % args.chunk,
+                   "engine": engine if engine == "fp64" else
+                   "fixed (FP64 state and pointwise physics; transforms in 64-bit block fixed point)",
+                   "value_other_engine": {other: alt},
                    "model_steps_per_step": args.chunk,
                    "model_steps_per_s": model_steps * world / total_s,
                    "l2": "flushed (256 MB write) before every timed step",
@@ -322,9 +370,10 @@ def run_ours(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
                      "peak_source": peak_kind,
-                     "kernel_ms": {"k_row_adv": row_ms, "k_col_fused": col_ms},
+                     "kernel_ms": {"k_row_adv" + sfx: row_ms, "k_col_fused" + sfx: col_ms},
                      "algorithmic_bytes_per_launch": nbytes,
-                     "note": "FP64 step: bound by the FP64 pipe, not HBM"},
+                     "note": "single nx=256 model: latency-bound (FP64 pipe / integer ALU "
+                             "under 55% busy, state L2-resident); see profiles/"},
         "cpu_baseline": base,
         "clocks": clocks.summary(),
         "gpu_launches": args.steps * (2 * args.chunk + 2),
@@ -335,9 +384,9 @@ def run_ours(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--chunk", type=int, default=100)
+    ap.add_argument("--chunk", type=int, default=500)
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--cpu-sample", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

@@ -93,9 +93,20 @@ int pqg_set_qy(pqg_plan *plan, const double *Qy);
 int pqg_set_filter(pqg_plan *plan, const double *filtr);
 int pqg_set_rek(pqg_plan *plan, double rek);
 
+/* Transform engine of the fused step (pqg_step), no counterpart in the
+ * reference: 0 = FP64 Stockham transforms (default); 1 = 64-bit block
+ * fixed-point transforms (exact integer additions, Q62 twiddles rounded to
+ * nearest, 50-52 bits below each sequence's largest element) with all
+ * pointwise physics in FP64.  Engine 1 takes the transforms off GB300's
+ * FP64 pipe; it needs power-of-two nx and ny.  pqg_get_engine returns the
+ * current engine (-1 for a NULL plan). */
+int pqg_set_engine(pqg_plan *plan, int engine);
+int pqg_get_engine(const pqg_plan *plan);
+
 /* Batched 2-D real transforms over `nplanes` (ny, nx) planes.
  * Replace the planned transforms and the fft/ifft helpers
- * (pyqg/kernel.pyx:208-267,291-309). */
+ * (pyqg/kernel.pyx:208-267,291-309).  Always FP64, whatever the plan's
+ * engine (which applies to the transforms inside the step). */
 int pqg_rfft2(pqg_plan *plan, const double *x, double *xh, int nplanes,
               void *stream);
 int pqg_irfft2(pqg_plan *plan, const double *xh, double *x, int nplanes,
@@ -147,6 +158,40 @@ int pqg_forward_timestep(pqg_plan *plan, int ablevel, double dt, double *qh,
  * t).  `aux` (may be NULL) receives the intermediates of the last step. */
 int pqg_step(pqg_plan *plan, pqg_state *state, int nsteps,
              const pqg_aux *aux, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Ensembles (no counterpart in the reference): B independent members of
+ * one shape (nz, ny, nx), physics shared except beta (Qy), bottom drag and
+ * background flow per member, advanced together by the fused step in FP32
+ * (precision 4) or FP64 (precision 8).  The ensemble owns its device
+ * state.  Grids: powers of two, 16..1024.
+ * ------------------------------------------------------------------- */
+typedef struct pqg_ens pqg_ens;
+
+const char *pqg_ens_last_error(void);
+int pqg_ens_create(pqg_ens **ens, int nmembers, int nz, int ny, int nx,
+                   int precision);
+int pqg_ens_destroy(pqg_ens *ens);
+/* shared constants (host, FP64; rounded once to the ensemble precision):
+ * a (nz, nz, nl, nk), kk (nk), ll (nl), filtr (nl, nk), time step dt */
+int pqg_ens_set_constants(pqg_ens *ens, const double *a, const double *kk,
+                          const double *ll, const double *filtr, double dt);
+/* per member (host, FP64): Ubg (B, nz), Qy (B, nz), rek (B) */
+int pqg_ens_set_members(pqg_ens *ens, const double *Ubg, const double *Qy,
+                        const double *rek);
+/* q (B, nz, ny, nx) FP64 host in/out; set_q also resets the AB3 history */
+int pqg_ens_set_q(pqg_ens *ens, const double *q, void *stream);
+int pqg_ens_get_q(pqg_ens *ens, double *q, void *stream);
+int pqg_ens_step(pqg_ens *ens, int nsteps, void *stream);
+/* several ensembles (e.g. one per grid size), each on its own stream
+ * branch so that they overlap on the GPU */
+int pqg_ens_step_many(pqg_ens **ens, int count, int nsteps, void *stream);
+/* FP64 sums per (member, layer): ke = 0.5 sum |kappa ph|^2 / M^2 and
+ * enstrophy 0.5 sum |qh|^2 / M^2 over the full spectral plane (host out) */
+int pqg_ens_energy(pqg_ens *ens, double *ke, double *enstrophy, void *stream);
+/* device pointers of the state (q, qh) and the step counter / time */
+int pqg_ens_state(pqg_ens *ens, void **q, void **qh, long long *tc,
+                  double *t);
 
 /* Instrumentation for the profile / bench tooling (no counterpart in the
  * reference): `nsteps` fused steps like pqg_step but launched one by one

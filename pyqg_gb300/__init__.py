@@ -13,5 +13,6 @@ from .sqg_model import SQGModel
 from .layered_model import LayeredModel
 from .parameterizations import *  # noqa: F401,F403
 from . import diagnostic_tools
+from .ensemble import Ensemble
 
 __version__ = "0.1.0"

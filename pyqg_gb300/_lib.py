@@ -46,6 +46,8 @@ SIGNATURES = {
     "pqg_set_qy": (_I, [_P, _P]),
     "pqg_set_filter": (_I, [_P, _P]),
     "pqg_set_rek": (_I, [_P, _D]),
+    "pqg_set_engine": (_I, [_P, _I]),
+    "pqg_get_engine": (_I, [_P]),
     "pqg_rfft2": (_I, [_P, _P, _P, _I, _P]),
     "pqg_irfft2": (_I, [_P, _P, _P, _I, _P]),
     "pqg_invert": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
@@ -59,6 +61,18 @@ SIGNATURES = {
     "pqg_step_profile": (_I, [_P, ctypes.POINTER(State), _I,
                               ctypes.POINTER(_D), ctypes.POINTER(_I), _P]),
     "pqg_rfft2_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
+    "pqg_ens_last_error": (ctypes.c_char_p, []),
+    "pqg_ens_create": (_I, [ctypes.POINTER(_P), _I, _I, _I, _I, _I]),
+    "pqg_ens_destroy": (_I, [_P]),
+    "pqg_ens_set_constants": (_I, [_P, _P, _P, _P, _P, _D]),
+    "pqg_ens_set_members": (_I, [_P, _P, _P, _P]),
+    "pqg_ens_set_q": (_I, [_P, _P, _P]),
+    "pqg_ens_get_q": (_I, [_P, _P, _P]),
+    "pqg_ens_step": (_I, [_P, _I, _P]),
+    "pqg_ens_step_many": (_I, [ctypes.POINTER(_P), _I, _I, _P]),
+    "pqg_ens_energy": (_I, [_P, _P, _P, _P]),
+    "pqg_ens_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                           ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_D)]),
 }
 
 _lock = threading.Lock()

@@ -37,21 +37,38 @@ def lib_path():
 
 
 def build(verbose=False, extra_flags=()):
-    """Compile the library; returns its path."""
+    """Compile each csrc/*.cu to an object in parallel, then link the
+    shared library; returns its path."""
+    from concurrent.futures import ThreadPoolExecutor
     os.makedirs(LIBDIR, exist_ok=True)
+    objdir = os.path.join(LIBDIR, "obj")
+    os.makedirs(objdir, exist_ok=True)
     out = lib_path()
     tmp = out + ".tmp"
-    cmd = [nvcc_path(), "-O3", "-std=c++17", "-shared", "-lineinfo",
-           "-gencode", "arch=compute_%s,code=sm_%s" % (ARCH, ARCH),
-           "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
-           "-Xptxas", "-O3",
-           "-I", os.path.join(os.path.dirname(HERE), "include"),
-           *extra_flags, *sources(), "-o", tmp]
-    res = subprocess.run(cmd, capture_output=True, text=True)
+    common = [nvcc_path(), "-O3", "-std=c++17", "-lineinfo",
+              "-gencode", "arch=compute_%s,code=sm_%s" % (ARCH, ARCH),
+              "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
+              "-Xptxas", "-O3",
+              "-I", os.path.join(os.path.dirname(HERE), "include"), *extra_flags]
+
+    def compile_one(src):
+        obj = os.path.join(objdir, os.path.basename(src)[:-3] + ".o")
+        res = subprocess.run(common + ["-c", src, "-o", obj], capture_output=True, text=True)
+        return src, obj, res
+
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        results = list(ex.map(compile_one, sources()))
+    for src, obj, res in results:
+        if verbose or res.returncode != 0:
+            sys.stderr.write(res.stdout + res.stderr)
+        if res.returncode != 0:
+            raise RuntimeError("nvcc failed on %s (exit %d)" % (src, res.returncode))
+    res = subprocess.run([nvcc_path(), "-shared", "-gencode", "arch=compute_%s,code=sm_%s" % (ARCH, ARCH),
+                          *[o for _, o, _ in results], "-o", tmp], capture_output=True, text=True)
     if verbose or res.returncode != 0:
         sys.stderr.write(res.stdout + res.stderr)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed (exit %d)" % res.returncode)
+        raise RuntimeError("nvcc link failed (exit %d)" % res.returncode)
     os.replace(tmp, out)
     return out
 

@@ -1,0 +1,856 @@
+// Batched ensembles of independent models on sm_103a, in FP32 or FP64.
+//
+// A group holds B members of one shape (nz, ny, nx) and one physics
+// (inversion matrix, filter, background flow), differing in beta (through
+// ikQy), bottom drag and initial state.  All members advance together: each
+// model step is two kernels over the whole group (rows of all members, then
+// columns of all members), so a group of small models fills the GPU.
+// Several groups (uneven sizes) advance in one CUDA graph per chunk of steps,
+// one graph branch per group.
+//
+// Precision forms: FP32 state, transforms, products and Adams-Bashforth
+// update (`float2`), with the inversion matrix and constants built in FP64
+// on the host and rounded once, and the energy / enstrophy sums accumulated
+// in FP64; or FP64 throughout (`double2`), which reproduces the single-model
+// FP64 step bit for bit.
+//
+// Layout (member-major): q (B, nz, ny, nx); qh and the tendencies
+// (B, nz, ny, nk); transposition scratch (B, 3 nz, ny, nk) (planes U, V, Q).
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pyqg_gb300.h"
+#include "pqg_fft.cuh"
+
+namespace cg = cooperative_groups;
+using namespace pqg;
+
+#define PQG_API __attribute__((visibility("default")))
+
+namespace {
+
+thread_local std::string e_last_error;
+int efail(int code, const std::string& msg) {
+  e_last_error = msg;
+  return code;
+}
+#define ECUDA(call)                                                                  \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) return efail(PQG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// pointwise physics, generic over the precision (the double2 versions are
+// the same operations as the single-model kernels)
+// ---------------------------------------------------------------------------
+template <class V, class S>
+__device__ __forceinline__ V g_ph_acc(V acc, S a, V q) { return mk(sfma(a, q.x, acc.x), sfma(a, q.y, acc.y)); }
+template <class V, class S>
+__device__ __forceinline__ V g_uh(S l, V ph) { return mk(smul(l, ph.y), -smul(l, ph.x)); }
+template <class V, class S>
+__device__ __forceinline__ V g_vh(S k, V ph) { return mk(-smul(k, ph.y), smul(k, ph.x)); }
+template <class V, class S>
+__device__ __forceinline__ V g_tendency(S k, S l, S kQy, V uqh, V vqh, V ph) {
+  const S re = sfma(kQy, ph.y, sfma(l, vqh.y, smul(k, uqh.y)));
+  const S im = sfma(kQy, ph.x, sfma(l, vqh.x, smul(k, uqh.x)));
+  return mk(re, -im);
+}
+template <class V, class S>
+__device__ __forceinline__ V g_friction(V dq, S rk2, V ph) { return mk(sfma(rk2, ph.x, dq.x), sfma(rk2, ph.y, dq.y)); }
+template <class V, class S>
+__device__ __forceinline__ V g_ab(S f, V qh, V dq, V dqp, V dqpp, S c1, S c2, S c3) {
+  const S re = sfma(c3, dqpp.x, sfma(c2, dqp.x, sfma(c1, dq.x, qh.x)));
+  const S im = sfma(c3, dqpp.y, sfma(c2, dqp.y, sfma(c1, dq.y, qh.y)));
+  return mk(smul(f, re), smul(f, im));
+}
+
+template <class V> struct Sc;
+template <> struct Sc<double2> { typedef double T; };
+template <> struct Sc<float2> { typedef float T; };
+
+struct EGeo {
+  int B, nz, ny, nx, nk, M;
+  size_t mstride;   // scratch complex values per member (3 nz ny nk)
+};
+
+template <class S>
+struct EConsts {
+  const S* a;      // (nz, nz, ny, nk)
+  const S* kk;     // (nk)
+  const S* ll;     // (ny)
+  const S* k2l2;   // (ny, nk)
+  const S* filtr;  // (ny, nk)
+  const S* kQy;    // (B, nz, nk)
+  const S* Ubg;    // (B, nz)
+  const S* rek;    // (B)
+};
+
+__device__ __forceinline__ size_t sidx(int b, int z, int l, int k, int nz, int ny, int nk) {
+  return (((size_t)b * nz + z) * ny + l) * nk + k;
+}
+
+// ---------------------------------------------------------------------------
+// row kernel: rows of all members; C2R of mixed U, V and Q (or physical q),
+// products, R2C of uq, vq back into the U, V planes
+// ---------------------------------------------------------------------------
+template <class V, int LOGM>
+__global__ void e_row_adv(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, const typename Sc<V>::T* qphys,
+                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb_) {
+  typedef typename Sc<V>::T S;
+  constexpr int M = 1 << LOGM;
+  extern __shared__ __align__(16) unsigned char esm[];
+  V* tw = reinterpret_cast<V*>(esm);
+  const int nk = M + 1, nx = 2 * M;
+  const int rows_m = g.nz * g.ny;
+  const int nrows = g.B * rows_m;
+  const int r0 = blockIdx.x * rb_;
+  const int rb = min(rb_, nrows - r0);
+  V* bU = tw + nx;
+  V* bV = bU + rb_ * M;
+  V* bQ = bV + rb_ * M;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
+  __syncthreads();
+  const int half = M / 2 + 1;
+  const size_t plane3 = (size_t)g.nz * g.ny * nk;
+  for (int t = threadIdx.x; t < 3 * rb * half; t += blockDim.x) {
+    const int f = t / (rb * half);
+    const int rem = t - f * rb * half;
+    const int rr = rem / half, k = rem - rr * half;
+    const int r = r0 + rr;
+    const int b = r / rows_m, rm = r - b * rows_m;
+    V* buf = (f == 0 ? bU : (f == 1 ? bV : bQ)) + rr * M;
+    if (f < 2 || !qphys) {
+      const V* X = scratch + b * g.mstride + f * plane3 + (size_t)rm * nk;
+      c2r_pre(X, buf, M, k, tw);
+    } else {
+      const V* row = reinterpret_cast<const V*>(qphys + (size_t)r * nx);
+      if (k < M - k) buf[k] = row[k];
+      if (k < M - k && M - 1 - k != k) buf[M - 1 - k] = row[M - 1 - k];
+    }
+  }
+  __syncthreads();
+  Pow2Fft<M, 1, true, V>::run(bU, M, (qphys ? 2 : 3) * rb_, tw, 2);
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    const int r = r0 + rr;
+    const int b = r / rows_m, z = (r - b * rows_m) / g.ny;
+    V u = cscale(bU[rr * M + m], scale), v = cscale(bV[rr * M + m], scale);
+    V q = bQ[rr * M + m];
+    if (!qphys) q = cscale(q, scale);
+    const S ub = c.Ubg[b * g.nz + z];
+    bU[rr * M + m] = mk(smul(sadd(u.x, ub), q.x), smul(sadd(u.y, ub), q.y));
+    bV[rr * M + m] = mk(smul(v.x, q.x), smul(v.y, q.y));
+  }
+  __syncthreads();
+  Pow2Fft<M, 1, false, V>::run(bU, M, 2 * rb_, tw, 2);
+  for (int t = threadIdx.x; t < 2 * rb * half; t += blockDim.x) {
+    const int f = t / (rb * half);
+    const int rem = t - f * rb * half;
+    const int rr = rem / half, k = rem - rr * half;
+    const int r = r0 + rr;
+    const int b = r / rows_m, rm = r - b * rows_m;
+    V* X = scratch + b * g.mstride + f * plane3 + (size_t)rm * nk;
+    r2c_post((f == 0 ? bU : bV) + rr * M, X, M, k, tw);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fused column kernel: grid (nz, ceil(nk / C), B), cluster (nz, 1, 1); each
+// CTA handles C consecutive columns of one layer of one member.  Shared:
+// [tw (ny)] [U: C][V: C][QN: C][QO: C] sequences of ny.
+// ---------------------------------------------------------------------------
+template <class V, int LOGN>
+__global__ void e_col_fused(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, V* qh, const V* dqp,
+                            V* dqpp, const V* __restrict__ twy, typename Sc<V>::T c1,
+                            typename Sc<V>::T c2, typename Sc<V>::T c3, int C) {
+  typedef typename Sc<V>::T S;
+  constexpr int N = 1 << LOGN;
+  extern __shared__ __align__(16) unsigned char esm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int ny = N, nk = g.nk, nz = g.nz;
+  const int z = blockIdx.x, k0 = blockIdx.y * C, b = blockIdx.z;
+  V* tw = reinterpret_cast<V*>(esm);
+  V* bU = tw + ny;
+  V* bV = bU + C * ny;
+  V* bQN = bV + C * ny;
+  V* bQO = bQN + C * ny;
+  const size_t plane = (size_t)ny * nk;
+  V* mU = scratch + b * g.mstride + (size_t)z * plane;
+  V* mV = mU + (size_t)nz * plane;
+  V* mQ = mV + (size_t)nz * plane;
+  for (int i = threadIdx.x; i < ny; i += blockDim.x) tw[i] = twy[i];
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    const bool ok = k < nk;
+    bU[cc * ny + l] = ok ? mU[(size_t)l * nk + k] : mk((S)0, (S)0);
+    bV[cc * ny + l] = ok ? mV[(size_t)l * nk + k] : mk((S)0, (S)0);
+    bQO[cc * ny + l] = ok ? qh[sidx(b, z, l, k, nz, ny, nk)] : mk((S)0, (S)0);
+  }
+  __syncthreads();
+  Pow2Fft<N, 1, false, V>::run(bU, ny, 2 * C, tw, 1);
+  cluster.sync();
+  const S rek = c.rek[b];
+  const bool drag = (rek != (S)0) && (z == nz - 1);
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    if (k >= nk) continue;
+    const int i = cc * ny + l;
+    const size_t o = sidx(b, z, l, k, nz, ny, nk);
+    V p = mk((S)0, (S)0);
+    for (int z1 = 0; z1 < nz; z1++) {
+      const V* rq = cluster.map_shared_rank(bQO, z1);
+      p = g_ph_acc(p, c.a[(((size_t)z * nz + z1) * ny + l) * nk + k], rq[i]);
+    }
+    const S kk = c.kk[k], kQy = c.kQy[((size_t)b * nz + z) * nk + k];
+    V d = g_tendency(kk, c.ll[l], kQy, bU[i], bV[i], p);
+    if (drag) d = g_friction(d, smul(rek, c.k2l2[(size_t)l * nk + k]), p);
+    const V pv = dqp[o], ppv = dqpp[o];
+    const V qn = g_ab(c.filtr[(size_t)l * nk + k], bQO[i], d, pv, ppv, c1, c2, c3);
+    qh[o] = qn;
+    dqpp[o] = d;   // the newest tendency takes the oldest one's buffer
+    bQN[i] = qn;
+  }
+  cluster.sync();
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    const int i = cc * ny + l;
+    if (k >= nk) { bU[i] = mk((S)0, (S)0); bV[i] = mk((S)0, (S)0); bQN[i] = mk((S)0, (S)0); continue; }
+    V p = mk((S)0, (S)0);
+    for (int z1 = 0; z1 < nz; z1++) {
+      const V* rq = cluster.map_shared_rank(bQN, z1);
+      p = g_ph_acc(p, c.a[(((size_t)z * nz + z1) * ny + l) * nk + k], rq[i]);
+    }
+    bU[i] = g_uh(c.ll[l], p);
+    bV[i] = g_vh(c.kk[k], p);
+  }
+  cluster.sync();
+  Pow2Fft<N, 1, true, V>::run(bU, ny, 3 * C, tw, 1);
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    if (k >= nk) continue;
+    const int i = cc * ny + l;
+    mU[(size_t)l * nk + k] = bU[i];
+    mV[(size_t)l * nk + k] = bV[i];
+    mQ[(size_t)l * nk + k] = bQN[i];
+  }
+}
+
+// prologue: mixed U, V of the current qh (grid (nz, ceil(nk / C), B))
+template <class V, int LOGN>
+__global__ void e_col_invert(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, const V* qh,
+                             const V* __restrict__ twy, int C) {
+  typedef typename Sc<V>::T S;
+  constexpr int N = 1 << LOGN;
+  extern __shared__ __align__(16) unsigned char esm[];
+  const int ny = N, nk = g.nk, nz = g.nz;
+  const int z = blockIdx.x, k0 = blockIdx.y * C, b = blockIdx.z;
+  V* tw = reinterpret_cast<V*>(esm);
+  V* bU = tw + ny;
+  V* bV = bU + C * ny;
+  const size_t plane = (size_t)ny * nk;
+  V* mU = scratch + b * g.mstride + (size_t)z * plane;
+  V* mV = mU + (size_t)nz * plane;
+  for (int i = threadIdx.x; i < ny; i += blockDim.x) tw[i] = twy[i];
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    const int i = cc * ny + l;
+    if (k >= nk) { bU[i] = mk((S)0, (S)0); bV[i] = mk((S)0, (S)0); continue; }
+    V p = mk((S)0, (S)0);
+    for (int z1 = 0; z1 < nz; z1++)
+      p = g_ph_acc(p, c.a[(((size_t)z * nz + z1) * ny + l) * nk + k], qh[sidx(b, z1, l, k, nz, ny, nk)]);
+    bU[i] = g_uh(c.ll[l], p);
+    bV[i] = g_vh(c.kk[k], p);
+  }
+  __syncthreads();
+  Pow2Fft<N, 1, true, V>::run(bU, ny, 2 * C, tw, 1);
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    if (k >= nk) continue;
+    mU[(size_t)l * nk + k] = bU[cc * ny + l];
+    mV[(size_t)l * nk + k] = bV[cc * ny + l];
+  }
+}
+
+// mixed plane `field` of every member -> physical (B, nz, ny, nx)
+template <class V, int LOGM>
+__global__ void e_row_c2r(EGeo g, const V* scratch, int field, typename Sc<V>::T* phys,
+                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb_) {
+  constexpr int M = 1 << LOGM;
+  extern __shared__ __align__(16) unsigned char esm[];
+  V* tw = reinterpret_cast<V*>(esm);
+  V* bq = tw + 2 * M;
+  const int nk = M + 1, nx = 2 * M;
+  const int rows_m = g.nz * g.ny, nrows = g.B * rows_m;
+  const int r0 = blockIdx.x * rb_;
+  const int rb = min(rb_, nrows - r0);
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
+  __syncthreads();
+  const int half = M / 2 + 1;
+  const size_t plane3 = (size_t)g.nz * g.ny * nk;
+  for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
+    const int rr = t / half, k = t - rr * half;
+    const int r = r0 + rr, b = r / rows_m, rm = r - b * rows_m;
+    c2r_pre(scratch + b * g.mstride + field * plane3 + (size_t)rm * nk, bq + rr * M, M, k, tw);
+  }
+  __syncthreads();
+  Pow2Fft<M, 1, true, V>::run(bq, M, rb_, tw, 2);
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    *reinterpret_cast<V*>(phys + (size_t)(r0 + rr) * nx + 2 * m) = cscale(bq[rr * M + m], scale);
+  }
+}
+
+// physical (B, nz, ny, nx) -> mixed plane 0 of every member
+template <class V, int LOGM>
+__global__ void e_row_r2c(EGeo g, V* scratch, const typename Sc<V>::T* phys, const V* __restrict__ twx, int rb_) {
+  constexpr int M = 1 << LOGM;
+  extern __shared__ __align__(16) unsigned char esm[];
+  V* tw = reinterpret_cast<V*>(esm);
+  V* bq = tw + 2 * M;
+  const int nk = M + 1, nx = 2 * M;
+  const int rows_m = g.nz * g.ny, nrows = g.B * rows_m;
+  const int r0 = blockIdx.x * rb_;
+  const int rb = min(rb_, nrows - r0);
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    bq[rr * M + m] = reinterpret_cast<const V*>(phys + (size_t)(r0 + rr) * nx)[m];
+  }
+  __syncthreads();
+  Pow2Fft<M, 1, false, V>::run(bq, M, rb_, tw, 2);
+  const int half = M / 2 + 1;
+  for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
+    const int rr = t / half, k = t - rr * half;
+    const int r = r0 + rr, b = r / rows_m, rm = r - b * rows_m;
+    r2c_post(bq + rr * M, scratch + b * g.mstride + (size_t)rm * nk, M, k, tw);
+  }
+}
+
+// mixed plane 0 -> spectral qh (grid (nz, ceil(nk / C), B))
+template <class V, int LOGN>
+__global__ void e_col_fwd(EGeo g, const V* scratch, V* qh, const V* __restrict__ twy, int C) {
+  typedef typename Sc<V>::T S;
+  constexpr int N = 1 << LOGN;
+  extern __shared__ __align__(16) unsigned char esm[];
+  const int ny = N, nk = g.nk, nz = g.nz;
+  const int z = blockIdx.x, k0 = blockIdx.y * C, b = blockIdx.z;
+  V* tw = reinterpret_cast<V*>(esm);
+  V* bq = tw + ny;
+  const V* m0 = scratch + b * g.mstride + (size_t)z * ny * nk;
+  for (int i = threadIdx.x; i < ny; i += blockDim.x) tw[i] = twy[i];
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    bq[cc * ny + l] = k < nk ? m0[(size_t)l * nk + k] : mk((S)0, (S)0);
+  }
+  __syncthreads();
+  Pow2Fft<N, 1, false, V>::run(bq, ny, C, tw, 1);
+  for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
+    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    if (k < nk) qh[sidx(b, z, l, k, nz, ny, nk)] = bq[cc * ny + l];
+  }
+}
+
+// precision conversions between an FP64 staging buffer and the state
+template <class S>
+__global__ void e_from_f64(const double* src, S* dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (S)src[i];
+}
+template <class S>
+__global__ void e_to_f64(const S* src, double* dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+
+// FP64 sums per (member, layer): kinetic energy 0.5 sum w |kappa ph|^2 / M^2
+// and enstrophy 0.5 sum w |qh|^2 / M^2, w = 2 for interior k columns and 1 at
+// k = 0 and k = nx/2 (half-plane spectrum).  Grid (nz, B), 256 threads.
+template <class V>
+__global__ void e_energy(EGeo g, EConsts<typename Sc<V>::T> c, const V* qh, double* ke, double* en,
+                         double inv_m2) {
+  const int z = blockIdx.x, b = blockIdx.y;
+  const int nz = g.nz, ny = g.ny, nk = g.nk;
+  double ske = 0.0, sen = 0.0;
+  for (int i = threadIdx.x; i < ny * nk; i += blockDim.x) {
+    const int l = i / nk, k = i - l * nk;
+    double pr = 0.0, pi = 0.0;
+    for (int z1 = 0; z1 < nz; z1++) {
+      const double a = (double)c.a[(((size_t)z * nz + z1) * ny + l) * nk + k];
+      const V q = qh[sidx(b, z1, l, k, nz, ny, nk)];
+      pr = fma(a, (double)q.x, pr);
+      pi = fma(a, (double)q.y, pi);
+    }
+    const V q = qh[sidx(b, z, l, k, nz, ny, nk)];
+    const double w = (k == 0 || k == nk - 1) ? 1.0 : 2.0;
+    const double k2 = (double)c.k2l2[(size_t)l * nk + k];
+    ske += w * k2 * (pr * pr + pi * pi);
+    sen += w * ((double)q.x * (double)q.x + (double)q.y * (double)q.y);
+  }
+  __shared__ double red[2][32];
+  for (int off = 16; off > 0; off >>= 1) {
+    ske += __shfl_xor_sync(0xffffffffu, ske, off);
+    sen += __shfl_xor_sync(0xffffffffu, sen, off);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][w] = ske; red[1][w] = sen; }
+  __syncthreads();
+  if (w == 0) {
+    ske = lane < (int)(blockDim.x >> 5) ? red[0][lane] : 0.0;
+    sen = lane < (int)(blockDim.x >> 5) ? red[1][lane] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) {
+      ske += __shfl_xor_sync(0xffffffffu, ske, off);
+      sen += __shfl_xor_sync(0xffffffffu, sen, off);
+    }
+    if (lane == 0) {
+      ke[(size_t)b * nz + z] = 0.5 * ske * inv_m2;
+      en[(size_t)b * nz + z] = 0.5 * sen * inv_m2;
+    }
+  }
+}
+
+}  // namespace
+
+// ===========================================================================
+// host side
+// ===========================================================================
+struct pqg_ens {
+  int B, nz, ny, nx, nk, M, prec;
+  size_t esz;  // scalar bytes
+  void* twx = nullptr; void* twy = nullptr;
+  void* a = nullptr; void* kk = nullptr; void* ll = nullptr; void* k2l2 = nullptr; void* filtr = nullptr;
+  void* kQy = nullptr; void* Ubg = nullptr; void* rek = nullptr;
+  void* q = nullptr; void* qh = nullptr; void* dq[3] = {nullptr, nullptr, nullptr};
+  void* scratch = nullptr;
+  double* d_red = nullptr;   // 2 B nz FP64 sums
+  int role_p = 1, role_pp = 2;
+  int ablevel = 0;
+  long long tc = 0;
+  double t = 0.0, dt = 0.0;
+  int T_row = 128, rb = 1, T_col = 128, C = 1;
+  std::vector<double> h_kk, h_Qy;  // for kQy
+  bool have_consts = false, have_members = false;
+};
+
+namespace {
+
+void cos_sin(int n, int m, long double& cr, long double& sr) {
+  const long double pi = 3.141592653589793238462643383279502884L;
+  long long num = 8LL * m, oct = num / n, rem = num - oct * n;
+  long double x = pi / 4 * (long double)rem / (long double)n;
+  long double c = cosl(x), s = sinl(x), y = pi / 4 - x;
+  switch (oct) {
+    case 0: cr = c; sr = s; break;
+    case 1: cr = sinl(y); sr = cosl(y); break;
+    case 2: cr = -s; sr = c; break;
+    case 3: cr = -cosl(y); sr = sinl(y); break;
+    case 4: cr = -c; sr = -s; break;
+    case 5: cr = -sinl(y); sr = -cosl(y); break;
+    case 6: cr = s; sr = -c; break;
+    default: cr = cosl(y); sr = -sinl(y); break;
+  }
+}
+
+int upload_scalars(pqg_ens* e, void* dst, const double* src, size_t n) {
+  if (e->prec == 8) {
+    ECUDA(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> f(n);
+    for (size_t i = 0; i < n; i++) f[i] = (float)src[i];
+    ECUDA(cudaMemcpy(dst, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  return PQG_OK;
+}
+
+int upload_twiddles(pqg_ens* e, void* dst, int n) {
+  std::vector<double> w(2 * (size_t)n);
+  for (int m = 0; m < n; m++) {
+    long double cr, sr;
+    cos_sin(n, m, cr, sr);
+    w[2 * m] = (double)cr;
+    w[2 * m + 1] = -(double)sr;
+  }
+  return upload_scalars(e, dst, w.data(), w.size());
+}
+
+bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+int lg2(int n) { int l = 0; while ((1 << l) < n) l++; return l; }
+
+#define E_LOGM(X) X(3) X(4) X(5) X(6) X(7) X(8) X(9)
+#define E_LOGN(X) X(4) X(5) X(6) X(7) X(8) X(9) X(10)
+
+template <class V>
+struct EK {
+  typedef typename Sc<V>::T S;
+  typedef void (*RowAdv)(EGeo, EConsts<S>, V*, const S*, const V*, S, int);
+  typedef void (*ColFused)(EGeo, EConsts<S>, V*, V*, const V*, V*, const V*, S, S, S, int);
+  typedef void (*ColInv)(EGeo, EConsts<S>, V*, const V*, const V*, int);
+  typedef void (*RowC2r)(EGeo, const V*, int, S*, const V*, S, int);
+  typedef void (*RowR2c)(EGeo, V*, const S*, const V*, int);
+  typedef void (*ColFwd)(EGeo, const V*, V*, const V*, int);
+  static RowAdv row_adv(int M) {
+    switch (lg2(M)) {
+#define C(L) case L: return e_row_adv<V, L>;
+      E_LOGM(C)
+#undef C
+      default: return nullptr;
+    }
+  }
+  static RowC2r row_c2r(int M) {
+    switch (lg2(M)) {
+#define C(L) case L: return e_row_c2r<V, L>;
+      E_LOGM(C)
+#undef C
+      default: return nullptr;
+    }
+  }
+  static RowR2c row_r2c(int M) {
+    switch (lg2(M)) {
+#define C(L) case L: return e_row_r2c<V, L>;
+      E_LOGM(C)
+#undef C
+      default: return nullptr;
+    }
+  }
+  static ColFused col_fused(int N) {
+    switch (lg2(N)) {
+#define C(L) case L: return e_col_fused<V, L>;
+      E_LOGN(C)
+#undef C
+      default: return nullptr;
+    }
+  }
+  static ColInv col_inv(int N) {
+    switch (lg2(N)) {
+#define C(L) case L: return e_col_invert<V, L>;
+      E_LOGN(C)
+#undef C
+      default: return nullptr;
+    }
+  }
+  static ColFwd col_fwd(int N) {
+    switch (lg2(N)) {
+#define C(L) case L: return e_col_fwd<V, L>;
+      E_LOGN(C)
+#undef C
+      default: return nullptr;
+    }
+  }
+};
+
+template <class V>
+EConsts<typename Sc<V>::T> econsts(const pqg_ens* e) {
+  typedef typename Sc<V>::T S;
+  EConsts<S> c;
+  c.a = (const S*)e->a; c.kk = (const S*)e->kk; c.ll = (const S*)e->ll; c.k2l2 = (const S*)e->k2l2;
+  c.filtr = (const S*)e->filtr; c.kQy = (const S*)e->kQy; c.Ubg = (const S*)e->Ubg; c.rek = (const S*)e->rek;
+  return c;
+}
+EGeo egeo(const pqg_ens* e) {
+  EGeo g;
+  g.B = e->B; g.nz = e->nz; g.ny = e->ny; g.nx = e->nx; g.nk = e->nk; g.M = e->M;
+  g.mstride = (size_t)3 * e->nz * e->ny * e->nk;
+  return g;
+}
+size_t vsz(const pqg_ens* e) { return 2 * e->esz; }
+
+template <class V>
+int launch_row_adv(pqg_ens* e, bool first, cudaStream_t st) {
+  typedef typename Sc<V>::T S;
+  const int nrows = e->B * e->nz * e->ny;
+  const size_t smem = vsz(e) * ((size_t)e->nx + 3 * (size_t)e->rb * e->M);
+  EK<V>::row_adv(e->M)<<<(nrows + e->rb - 1) / e->rb, e->T_row, smem, st>>>(
+      egeo(e), econsts<V>(e), (V*)e->scratch, first ? (const S*)e->q : nullptr, (const V*)e->twx,
+      (S)(1.0 / ((double)e->nx * e->ny)), e->rb);
+  ECUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
+template <class V>
+int launch_col_fused(pqg_ens* e, cudaStream_t st) {
+  typedef typename Sc<V>::T S;
+  double c1, c2, c3;
+  if (e->ablevel <= 0) { c1 = e->dt; c2 = 0.0; c3 = 0.0; }
+  else if (e->ablevel == 1) { c1 = 1.5 * e->dt; c2 = -0.5 * e->dt; c3 = 0.0; }
+  else { c1 = 23. / 12. * e->dt; c2 = -16. / 12. * e->dt; c3 = 5. / 12. * e->dt; }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(e->nz, (e->nk + e->C - 1) / e->C, e->B);
+  cfg.blockDim = dim3(e->T_col, 1, 1);
+  cfg.dynamicSmemBytes = vsz(e) * (size_t)e->ny * (1 + 4 * e->C);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = e->nz;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ECUDA(cudaLaunchKernelEx(&cfg, EK<V>::col_fused(e->ny), egeo(e), econsts<V>(e), (V*)e->scratch, (V*)e->qh,
+                           (const V*)e->dq[e->role_p], (V*)e->dq[e->role_pp], (const V*)e->twy, (S)c1, (S)c2,
+                           (S)c3, e->C));
+  // rotation: newest tendency in the old pp buffer
+  std::swap(e->role_p, e->role_pp);
+  e->ablevel = e->ablevel >= 2 ? 2 : e->ablevel + 1;
+  e->tc += 1;
+  e->t += e->dt;
+  return PQG_OK;
+}
+
+template <class V>
+int launch_prologue(pqg_ens* e, cudaStream_t st) {
+  EK<V>::col_inv(e->ny)<<<dim3(e->nz, (e->nk + e->C - 1) / e->C, e->B), e->T_col,
+                           vsz(e) * (size_t)e->ny * (1 + 2 * e->C), st>>>(
+      egeo(e), econsts<V>(e), (V*)e->scratch, (const V*)e->qh, (const V*)e->twy, e->C);
+  ECUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
+template <class V>
+int launch_epilogue(pqg_ens* e, cudaStream_t st) {
+  typedef typename Sc<V>::T S;
+  const int nrows = e->B * e->nz * e->ny;
+  const size_t smem = vsz(e) * ((size_t)e->nx + (size_t)e->rb * e->M);
+  EK<V>::row_c2r(e->M)<<<(nrows + e->rb - 1) / e->rb, e->T_row, smem, st>>>(
+      egeo(e), (const V*)e->scratch, 2, (S*)e->q, (const V*)e->twx, (S)(1.0 / ((double)e->nx * e->ny)), e->rb);
+  ECUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
+template <class V>
+int step_impl(pqg_ens* e, int nsteps, cudaStream_t st) {
+  int rc = launch_prologue<V>(e, st);
+  for (int i = 0; i < nsteps && !rc; i++) {
+    rc = launch_row_adv<V>(e, i == 0, st);
+    if (!rc) rc = launch_col_fused<V>(e, st);
+  }
+  if (!rc) rc = launch_epilogue<V>(e, st);
+  return rc;
+}
+
+template <class V>
+int set_q_impl(pqg_ens* e, cudaStream_t st) {
+  // staging FP64 q is in scratch; convert to the state precision, then
+  // qh = rfft2(q) through mixed plane 0
+  typedef typename Sc<V>::T S;
+  const size_t n = (size_t)e->B * e->nz * e->ny * e->nx;
+  e_from_f64<S><<<1024, 256, 0, st>>>((const double*)e->scratch, (S*)e->q, n);
+  ECUDA(cudaGetLastError());
+  const int nrows = e->B * e->nz * e->ny;
+  EK<V>::row_r2c(e->M)<<<(nrows + e->rb - 1) / e->rb, e->T_row, vsz(e) * ((size_t)e->nx + (size_t)e->rb * e->M), st>>>(
+      egeo(e), (V*)e->scratch, (const S*)e->q, (const V*)e->twx, e->rb);
+  ECUDA(cudaGetLastError());
+  EK<V>::col_fwd(e->ny)<<<dim3(e->nz, (e->nk + e->C - 1) / e->C, e->B), e->T_col,
+                           vsz(e) * (size_t)e->ny * (1 + e->C), st>>>(
+      egeo(e), (const V*)e->scratch, (V*)e->qh, (const V*)e->twy, e->C);
+  ECUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
+template <class V>
+int set_attrs(pqg_ens* e) {
+  const int big = 200 * 1024;
+  ECUDA(cudaFuncSetAttribute(EK<V>::row_adv(e->M), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  ECUDA(cudaFuncSetAttribute(EK<V>::row_c2r(e->M), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  ECUDA(cudaFuncSetAttribute(EK<V>::row_r2c(e->M), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  ECUDA(cudaFuncSetAttribute(EK<V>::col_fused(e->ny), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  ECUDA(cudaFuncSetAttribute(EK<V>::col_inv(e->ny), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  ECUDA(cudaFuncSetAttribute(EK<V>::col_fwd(e->ny), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  return PQG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+PQG_API const char* pqg_ens_last_error(void) { return e_last_error.c_str(); }
+
+PQG_API int pqg_ens_create(pqg_ens** out, int nmembers, int nz, int ny, int nx, int precision) {
+  if (!out) return efail(PQG_ERR_INVALID, "output pointer is NULL");
+  *out = nullptr;
+  if (nmembers < 1 || nz < 1 || nz > 8) return efail(PQG_ERR_INVALID, "need nmembers >= 1 and 1 <= nz <= 8");
+  if (precision != 4 && precision != 8) return efail(PQG_ERR_INVALID, "precision must be 4 (FP32) or 8 (FP64)");
+  if (!pow2(nx) || !pow2(ny) || nx < 16 || nx > 1024 || ny < 16 || ny > 1024)
+    return efail(PQG_ERR_UNSUPPORTED, "ensemble grids must be powers of two, 16..1024");
+  pqg_ens* e = new pqg_ens();
+  e->B = nmembers; e->nz = nz; e->ny = ny; e->nx = nx; e->nk = nx / 2 + 1; e->M = nx / 2;
+  e->prec = precision; e->esz = precision;
+  e->rb = std::max(1, std::min(16, 256 / e->M));
+  e->T_row = std::max(64, std::min(256, e->rb * e->M / 2));
+  e->C = std::max(1, std::min(8, 512 / ny));
+  e->T_col = std::max(64, std::min(256, ny * e->C / 2));
+  if (const char* s = getenv("PQG_ENS_C")) e->C = atoi(s);
+  if (const char* s = getenv("PQG_ENS_T_ROW")) e->T_row = atoi(s);
+  if (const char* s = getenv("PQG_ENS_RB")) e->rb = atoi(s);
+  if (const char* s = getenv("PQG_ENS_T_COL")) e->T_col = atoi(s);
+  const size_t S = (size_t)nmembers * nz * ny * e->nk, P = (size_t)nmembers * nz * ny * nx;
+  const size_t V = 2 * e->esz;
+  bool ok = true;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (!ok) return;
+    ok = cudaMalloc(p, bytes) == cudaSuccess && cudaMemset(*p, 0, bytes) == cudaSuccess;
+  };
+  alloc(&e->twx, V * nx); alloc(&e->twy, V * ny);
+  alloc(&e->a, e->esz * nz * nz * ny * e->nk); alloc(&e->kk, e->esz * e->nk); alloc(&e->ll, e->esz * ny);
+  alloc(&e->k2l2, e->esz * ny * e->nk); alloc(&e->filtr, e->esz * ny * e->nk);
+  alloc(&e->kQy, e->esz * nmembers * nz * e->nk); alloc(&e->Ubg, e->esz * nmembers * nz);
+  alloc(&e->rek, e->esz * nmembers);
+  alloc(&e->q, e->esz * P); alloc(&e->qh, V * S);
+  for (int i = 0; i < 3; i++) alloc(&e->dq[i], V * S);
+  alloc(&e->scratch, std::max(V * 3 * S, sizeof(double) * P));
+  alloc((void**)&e->d_red, sizeof(double) * 2 * nmembers * nz);
+  if (!ok) { pqg_ens_destroy(e); return efail(PQG_ERR_NOMEM, "cudaMalloc failed in pqg_ens_create"); }
+  int rc = upload_twiddles(e, e->twx, nx);
+  if (!rc) rc = upload_twiddles(e, e->twy, ny);
+  if (!rc) rc = precision == 4 ? set_attrs<float2>(e) : set_attrs<double2>(e);
+  if (rc) { pqg_ens_destroy(e); return rc; }
+  *out = e;
+  return PQG_OK;
+}
+
+PQG_API int pqg_ens_destroy(pqg_ens* e) {
+  if (!e) return PQG_OK;
+  void* ps[] = {e->twx, e->twy, e->a, e->kk, e->ll, e->k2l2, e->filtr, e->kQy, e->Ubg, e->rek, e->q,
+                e->qh, e->dq[0], e->dq[1], e->dq[2], e->scratch, e->d_red};
+  for (void* p : ps) cudaFree(p);
+  delete e;
+  return PQG_OK;
+}
+
+PQG_API int pqg_ens_set_constants(pqg_ens* e, const double* a, const double* kk, const double* ll,
+                                  const double* filtr, double dt) {
+  if (!e || !a || !kk || !ll || !filtr) return efail(PQG_ERR_INVALID, "NULL argument");
+  const int nk = e->nk, ny = e->ny;
+  int rc = upload_scalars(e, e->a, a, (size_t)e->nz * e->nz * ny * nk);
+  if (!rc) rc = upload_scalars(e, e->kk, kk, nk);
+  if (!rc) rc = upload_scalars(e, e->ll, ll, ny);
+  if (!rc) rc = upload_scalars(e, e->filtr, filtr, (size_t)ny * nk);
+  if (rc) return rc;
+  std::vector<double> k2l2((size_t)ny * nk);
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nk; i++) {
+      const double x = kk[i] * kk[i], y = ll[j] * ll[j];
+      k2l2[(size_t)j * nk + i] = x + y;
+    }
+  rc = upload_scalars(e, e->k2l2, k2l2.data(), k2l2.size());
+  if (rc) return rc;
+  e->h_kk.assign(kk, kk + nk);
+  e->dt = dt;
+  e->ablevel = 0;
+  e->have_consts = true;
+  return PQG_OK;
+}
+
+PQG_API int pqg_ens_set_members(pqg_ens* e, const double* Ubg, const double* Qy, const double* rek) {
+  if (!e || !Ubg || !Qy || !rek) return efail(PQG_ERR_INVALID, "NULL argument");
+  if (!e->have_consts) return efail(PQG_ERR_STATE, "set the shared constants first");
+  const int B = e->B, nz = e->nz, nk = e->nk;
+  std::vector<double> kqy((size_t)B * nz * nk);
+  for (int b = 0; b < B; b++)
+    for (int z = 0; z < nz; z++)
+      for (int i = 0; i < nk; i++) kqy[((size_t)b * nz + z) * nk + i] = e->h_kk[i] * Qy[(size_t)b * nz + z];
+  int rc = upload_scalars(e, e->kQy, kqy.data(), kqy.size());
+  if (!rc) rc = upload_scalars(e, e->Ubg, Ubg, (size_t)B * nz);
+  if (!rc) rc = upload_scalars(e, e->rek, rek, B);
+  if (!rc) e->have_members = true;
+  return rc;
+}
+
+PQG_API int pqg_ens_set_q(pqg_ens* e, const double* q_host, void* stream) {
+  if (!e || !q_host) return efail(PQG_ERR_INVALID, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n = (size_t)e->B * e->nz * e->ny * e->nx;
+  ECUDA(cudaMemcpyAsync(e->scratch, q_host, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  int rc = e->prec == 4 ? set_q_impl<float2>(e, st) : set_q_impl<double2>(e, st);
+  if (rc) return rc;
+  ECUDA(cudaStreamSynchronize(st));
+  for (int i = 0; i < 3; i++) ECUDA(cudaMemset(e->dq[i], 0, 2 * e->esz * (size_t)e->B * e->nz * e->ny * e->nk));
+  e->ablevel = 0;
+  e->role_p = 1;
+  e->role_pp = 2;
+  return PQG_OK;
+}
+
+PQG_API int pqg_ens_get_q(pqg_ens* e, double* q_host, void* stream) {
+  if (!e || !q_host) return efail(PQG_ERR_INVALID, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n = (size_t)e->B * e->nz * e->ny * e->nx;
+  if (e->prec == 4) e_to_f64<float><<<1024, 256, 0, st>>>((const float*)e->q, (double*)e->scratch, n);
+  else e_to_f64<double><<<1024, 256, 0, st>>>((const double*)e->q, (double*)e->scratch, n);
+  ECUDA(cudaGetLastError());
+  ECUDA(cudaMemcpyAsync(q_host, e->scratch, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ECUDA(cudaStreamSynchronize(st));
+  return PQG_OK;
+}
+
+PQG_API int pqg_ens_step(pqg_ens* e, int nsteps, void* stream) {
+  if (!e || nsteps < 0) return efail(PQG_ERR_INVALID, "bad argument to pqg_ens_step");
+  if (!e->have_consts || !e->have_members) return efail(PQG_ERR_STATE, "constants or members not set");
+  if (nsteps == 0) return PQG_OK;
+  return e->prec == 4 ? step_impl<float2>(e, nsteps, (cudaStream_t)stream)
+                      : step_impl<double2>(e, nsteps, (cudaStream_t)stream);
+}
+
+// All groups advance `nsteps` steps; each group on its own captured stream
+// branch so that groups overlap on the GPU; replayed as one graph per call.
+PQG_API int pqg_ens_step_many(pqg_ens** es, int count, int nsteps, void* stream) {
+  if (!es || count < 1 || nsteps < 0) return efail(PQG_ERR_INVALID, "bad argument to pqg_ens_step_many");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (count == 1) return pqg_ens_step(es[0], nsteps, stream);
+  std::vector<cudaStream_t> br(count);
+  std::vector<cudaEvent_t> done(count);
+  cudaEvent_t fork;
+  ECUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  for (int i = 0; i < count; i++) {
+    ECUDA(cudaStreamCreateWithFlags(&br[i], cudaStreamNonBlocking));
+    ECUDA(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming));
+  }
+  int rc = PQG_OK;
+  ECUDA(cudaEventRecord(fork, st));
+  for (int i = 0; i < count && !rc; i++) {
+    ECUDA(cudaStreamWaitEvent(br[i], fork, 0));
+    rc = pqg_ens_step(es[i], nsteps, br[i]);
+    ECUDA(cudaEventRecord(done[i], br[i]));
+  }
+  for (int i = 0; i < count; i++) cudaStreamWaitEvent(st, done[i], 0);
+  for (int i = 0; i < count; i++) {
+    cudaStreamDestroy(br[i]);
+    cudaEventDestroy(done[i]);
+  }
+  cudaEventDestroy(fork);
+  return rc;
+}
+
+PQG_API int pqg_ens_energy(pqg_ens* e, double* ke, double* ens, void* stream) {
+  if (!e || !ke || !ens) return efail(PQG_ERR_INVALID, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const double m2 = (double)e->nx * e->ny;
+  const double inv_m2 = 1.0 / (m2 * m2);
+  double* dk = e->d_red;
+  double* de = e->d_red + (size_t)e->B * e->nz;
+  if (e->prec == 4)
+    e_energy<float2><<<dim3(e->nz, e->B), 256, 0, st>>>(egeo(e), econsts<float2>(e), (const float2*)e->qh, dk, de, inv_m2);
+  else
+    e_energy<double2><<<dim3(e->nz, e->B), 256, 0, st>>>(egeo(e), econsts<double2>(e), (const double2*)e->qh, dk, de, inv_m2);
+  ECUDA(cudaGetLastError());
+  ECUDA(cudaMemcpyAsync(ke, dk, sizeof(double) * e->B * e->nz, cudaMemcpyDeviceToHost, st));
+  ECUDA(cudaMemcpyAsync(ens, de, sizeof(double) * e->B * e->nz, cudaMemcpyDeviceToHost, st));
+  ECUDA(cudaStreamSynchronize(st));
+  return PQG_OK;
+}
+
+PQG_API int pqg_ens_state(pqg_ens* e, void** q, void** qh, long long* tc, double* t) {
+  if (!e) return efail(PQG_ERR_INVALID, "NULL argument");
+  if (q) *q = e->q;
+  if (qh) *qh = e->qh;
+  if (tc) *tc = e->tc;
+  if (t) *t = e->t;
+  return PQG_OK;
+}
+
+}  // extern "C"

@@ -51,6 +51,33 @@ __device__ __forceinline__ double2 rot(double2 a) {
   return INV ? make_double2(-a.y, a.x) : make_double2(a.y, -a.x);
 }
 
+// Scalar operations with pinned rounding, overloaded on the precision, and
+// the float2 (FP32) counterparts of the complex helpers above.
+__device__ __forceinline__ double sadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ssub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double smul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double sfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float sadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float ssub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float smul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float sfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double2 mk(double x, double y) { return make_double2(x, y); }
+__device__ __forceinline__ float2 mk(float x, float y) { return make_float2(x, y); }
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(__fmul_rn(a.x, s), __fmul_rn(a.y, s)); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 w) {
+  return make_float2(__fmaf_rn(a.x, w.x, -__fmul_rn(a.y, w.y)), __fmaf_rn(a.x, w.y, __fmul_rn(a.y, w.x)));
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 w) {
+  return make_float2(__fmaf_rn(a.x, w.x, __fmul_rn(a.y, w.y)), __fmaf_rn(a.y, w.x, -__fmul_rn(a.x, w.y)));
+}
+template <bool INV>
+__device__ __forceinline__ float2 rot(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
 // Correctly rounded constants.
 constexpr double kSqrt3_2 = 0x1.bb67ae8584caap-1;  // sin(2 pi / 3)
 constexpr double kSqrt2_2 = 0x1.6a09e667f3bcdp-1;  // cos(pi / 4)
@@ -65,17 +92,19 @@ constexpr double kS5_2 = 0x1.2cf2304755a5ep-1;     // sin(4 pi / 5)
 template <int R, bool INV> struct Dft;
 
 template <bool INV> struct Dft<2, INV> {
-  static __device__ __forceinline__ void run(double2* v) {
-    double2 a = v[0], b = v[1];
+  template <class V>
+  static __device__ __forceinline__ void run(V* v) {
+    V a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
   }
 };
 
 template <bool INV> struct Dft<4, INV> {
-  static __device__ __forceinline__ void run(double2* v) {
-    double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-    double2 c = cadd(v[1], v[3]), d = rot<INV>(csub(v[1], v[3]));
+  template <class V>
+  static __device__ __forceinline__ void run(V* v) {
+    V a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    V c = cadd(v[1], v[3]), d = rot<INV>(csub(v[1], v[3]));
     v[0] = cadd(a, c);
     v[2] = csub(a, c);
     v[1] = cadd(b, d);
@@ -119,23 +148,22 @@ template <bool INV> struct Dft<5, INV> {
 };
 
 template <bool INV> struct Dft<8, INV> {
-  static __device__ __forceinline__ void run(double2* v) {
-    double2 e[4] = {v[0], v[2], v[4], v[6]};
-    double2 o[4] = {v[1], v[3], v[5], v[7]};
+  template <class V>
+  static __device__ __forceinline__ void run(V* v) {
+    typedef decltype(v[0].x) S;
+    const S h = (S)kSqrt2_2;
+    V e[4] = {v[0], v[2], v[4], v[6]};
+    V o[4] = {v[1], v[3], v[5], v[7]};
     Dft<4, INV>::run(e);
     Dft<4, INV>::run(o);
     // o1 *= w8, o2 *= w8^2 (= -+i), o3 *= w8^3, w8 = exp(-+ i pi / 4)
-    double2 t = o[1];
-    o[1] = INV ? make_double2(__dmul_rn(__dsub_rn(t.x, t.y), kSqrt2_2),
-                              __dmul_rn(__dadd_rn(t.x, t.y), kSqrt2_2))
-               : make_double2(__dmul_rn(__dadd_rn(t.x, t.y), kSqrt2_2),
-                              __dmul_rn(__dsub_rn(t.y, t.x), kSqrt2_2));
+    V t = o[1];
+    o[1] = INV ? mk(smul(ssub(t.x, t.y), h), smul(sadd(t.x, t.y), h))
+               : mk(smul(sadd(t.x, t.y), h), smul(ssub(t.y, t.x), h));
     o[2] = rot<INV>(o[2]);
     t = o[3];
-    o[3] = INV ? make_double2(__dmul_rn(-__dadd_rn(t.x, t.y), kSqrt2_2),
-                              __dmul_rn(__dsub_rn(t.x, t.y), kSqrt2_2))
-               : make_double2(__dmul_rn(__dsub_rn(t.y, t.x), kSqrt2_2),
-                              __dmul_rn(-__dadd_rn(t.x, t.y), kSqrt2_2));
+    o[3] = INV ? mk(smul(-sadd(t.x, t.y), h), smul(ssub(t.x, t.y), h))
+               : mk(smul(ssub(t.y, t.x), h), smul(-sadd(t.x, t.y), h));
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       v[r] = cadd(e[r], o[r]);
@@ -153,10 +181,10 @@ template <int R> struct MaxIt { static constexpr int value = R == 2 ? 4 : (R == 
 // One Stockham stage (radix R, Ns = product of earlier radices) on `nseq`
 // sequences of length n at buf + s*stride, in place through registers.
 // Twiddles come from a table tw[m*twstep] = exp(-2 pi i m / n).
-template <int R, bool INV>
-__device__ __forceinline__ void fft_stage(double2* buf, int stride, int nseq,
+template <int R, bool INV, class V>
+__device__ __forceinline__ void fft_stage(V* buf, int stride, int nseq,
                                           int n, int Ns,
-                                          const double2* __restrict__ tw,
+                                          const V* __restrict__ tw,
                                           int twstep) {
   constexpr int IT = MaxIt<R>::value;
   const int nb = n / R;
@@ -166,13 +194,13 @@ __device__ __forceinline__ void fft_stage(double2* buf, int stride, int nseq,
   const int tscale = (n / (Ns * R)) * twstep;
   for (int s0 = 0; s0 < nseq; s0 += per_round) {
     const int total = min(per_round, nseq - s0) * nb;
-    double2 v[IT][R];
+    V v[IT][R];
 #pragma unroll
     for (int it = 0; it < IT; it++) {
       const int p = tid + it * T;
       if (p < total) {
         const int sq = s0 + p / nb, j = p - (p / nb) * nb;
-        const double2* src = buf + sq * stride + j;
+        const V* src = buf + sq * stride + j;
 #pragma unroll
         for (int r = 0; r < R; r++) v[it][r] = src[r * nb];
       }
@@ -188,12 +216,12 @@ __device__ __forceinline__ void fft_stage(double2* buf, int stride, int nseq,
           const int ts = tscale * jm;
 #pragma unroll
           for (int r = 1; r < R; r++) {
-            const double2 w = tw[r * ts];
+            const V w = tw[r * ts];
             v[it][r] = INV ? cmulc(v[it][r], w) : cmul(v[it][r], w);
           }
         }
         Dft<R, INV>::run(v[it]);
-        double2* dst = buf + sq * stride + (j - jm) * R + jm;
+        V* dst = buf + sq * stride + (j - jm) * R + jm;
 #pragma unroll
         for (int r = 0; r < R; r++) dst[r * Ns] = v[it][r];
       }
@@ -235,18 +263,18 @@ __host__ __device__ constexpr int pow2_radix(int a, int s) {
 }
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
 
-template <int N, int NS, bool INV>
+template <int N, int NS, bool INV, class V = double2>
 struct Pow2Fft {
   static constexpr int R = pow2_radix(ilog2(N), ilog2(NS));
-  static __device__ __forceinline__ void run(double2* buf, int stride, int nseq,
-                                             const double2* __restrict__ tw, int twstep) {
+  static __device__ __forceinline__ void run(V* buf, int stride, int nseq,
+                                             const V* __restrict__ tw, int twstep) {
     fft_stage<R, INV>(buf, stride, nseq, N, NS, tw, twstep);
-    Pow2Fft<N, NS * R, INV>::run(buf, stride, nseq, tw, twstep);
+    Pow2Fft<N, NS * R, INV, V>::run(buf, stride, nseq, tw, twstep);
   }
 };
-template <int N, bool INV>
-struct Pow2Fft<N, N, INV> {
-  static __device__ __forceinline__ void run(double2*, int, int, const double2*, int) {}
+template <int N, bool INV, class V>
+struct Pow2Fft<N, N, INV, V> {
+  static __device__ __forceinline__ void run(V*, int, int, const V*, int) {}
 };
 
 // FFT engines used as kernel template arguments: a runtime mixed-radix plan,
@@ -276,42 +304,44 @@ struct FftPow2 {
 // (global) build Z'[k] and Z'[M-k] such that the unnormalised inverse
 // length-M FFT of Z' gives N * (x[2m] + i x[2m+1]).  The imaginary parts of
 // X[0] and X[M] are ignored (numpy.fft.irfft / FFTW c2r behaviour).
-__device__ __forceinline__ void c2r_pre(const double2* __restrict__ X,
-                                        double2* z, int M, int k,
-                                        const double2* __restrict__ tw) {
+template <class V>
+__device__ __forceinline__ void c2r_pre(const V* __restrict__ X,
+                                        V* z, int M, int k,
+                                        const V* __restrict__ tw) {
   if (k == 0) {
-    const double x0 = X[0].x, xm = X[M].x;
-    z[0] = make_double2(__dadd_rn(x0, xm), __dsub_rn(x0, xm));
+    const auto x0 = X[0].x, xm = X[M].x;
+    z[0] = mk(sadd(x0, xm), ssub(x0, xm));
     return;
   }
-  const double2 a = X[k], bb = X[M - k];
-  const double2 b = make_double2(bb.x, -bb.y);
-  const double2 A = cadd(a, b), B = csub(a, b);
-  const double2 D = cmulc(B, tw[k]);
-  z[k] = make_double2(__dsub_rn(A.x, D.y), __dadd_rn(A.y, D.x));
-  if (k != M - k) z[M - k] = make_double2(__dadd_rn(A.x, D.y), __dsub_rn(D.x, A.y));
+  const V a = X[k], bb = X[M - k];
+  const V b = mk(bb.x, -bb.y);
+  const V A = cadd(a, b), B = csub(a, b);
+  const V D = cmulc(B, tw[k]);
+  z[k] = mk(ssub(A.x, D.y), sadd(A.y, D.x));
+  if (k != M - k) z[M - k] = mk(sadd(A.x, D.y), ssub(D.x, A.y));
 }
 
 // R2C post-processing, task k in [0, M/2]: from Z = FFT_M(x[2m] + i x[2m+1])
 // (shared) write the half spectrum X[k], X[M-k] (and X[0], X[M] for k = 0).
-__device__ __forceinline__ void r2c_post(const double2* z,
-                                         double2* __restrict__ X, int M, int k,
-                                         const double2* __restrict__ tw) {
+template <class V>
+__device__ __forceinline__ void r2c_post(const V* z,
+                                         V* __restrict__ X, int M, int k,
+                                         const V* __restrict__ tw) {
+  typedef decltype(z[0].x) S;
+  const S half = (S)0.5;
   if (k == 0) {
-    const double2 z0 = z[0];
-    X[0] = make_double2(__dadd_rn(z0.x, z0.y), 0.0);
-    X[M] = make_double2(__dsub_rn(z0.x, z0.y), 0.0);
+    const V z0 = z[0];
+    X[0] = mk(sadd(z0.x, z0.y), (S)0);
+    X[M] = mk(ssub(z0.x, z0.y), (S)0);
     return;
   }
-  const double2 a = z[k], bb = z[M - k];
-  const double2 b = make_double2(bb.x, -bb.y);
-  const double2 A = cadd(a, b), B = csub(a, b);
-  const double2 C = cmul(B, tw[k]);
-  X[k] = make_double2(__dmul_rn(0.5, __dadd_rn(A.x, C.y)),
-                      __dmul_rn(0.5, __dsub_rn(A.y, C.x)));
+  const V a = z[k], bb = z[M - k];
+  const V b = mk(bb.x, -bb.y);
+  const V A = cadd(a, b), B = csub(a, b);
+  const V C = cmul(B, tw[k]);
+  X[k] = mk(smul(half, sadd(A.x, C.y)), smul(half, ssub(A.y, C.x)));
   if (k != M - k)
-    X[M - k] = make_double2(__dmul_rn(0.5, __dsub_rn(A.x, C.y)),
-                            __dmul_rn(-0.5, __dadd_rn(A.y, C.x)));
+    X[M - k] = mk(smul(half, ssub(A.x, C.y)), smul(-half, sadd(A.y, C.x)));
 }
 
 // ---------------------------------------------------------------------------

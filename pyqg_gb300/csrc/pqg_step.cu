@@ -31,6 +31,7 @@
 
 #include "../../include/pyqg_gb300.h"
 #include "pqg_fft.cuh"
+#include "pqg_fixed.cuh"
 
 namespace cg = cooperative_groups;
 using namespace pqg;
@@ -245,35 +246,75 @@ __device__ __forceinline__ size_t cidx(int plane, int l, int k, int ny, int nk) 
   return ((size_t)plane * ny + l) * nk + k;
 }
 
+// Column engines: how a CTA transforms `nseq` columns of length ny held in
+// shared memory (contiguous, stride ny).  ColRT: FP64 Stockham with the
+// runtime plan.  ColFx<LOGN>: 64-bit block fixed point (pqg_fixed.cuh).
+// `tw` is the shared twiddle table the engine loaded, `ws` 8 shared ints.
+struct ColRT {
+  static __device__ __forceinline__ void load(void* tw, const Geo& g, const longlong2*) {
+    load_tw(reinterpret_cast<double2*>(tw), g.twy, g.ny);
+  }
+  template <bool INV>
+  static __device__ __forceinline__ void run(double2* buf, int nseq, const Geo& g, const void* tw, int*) {
+    fft_run<INV>(buf, g.ny, nseq, g.fy, reinterpret_cast<const double2*>(tw), 1);
+  }
+};
+
+template <int LOGN>
+struct ColFx {
+  static constexpr int N = 1 << LOGN;
+  static constexpr int G = LOGN + 2;   // growth headroom of a length-N transform
+  static __device__ __forceinline__ void load(void* tw, const Geo&, const longlong2* twq) {
+    longlong2* t = reinterpret_cast<longlong2*>(tw);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) t[i] = twq[i];
+  }
+  template <bool INV>
+  static __device__ __forceinline__ void run(double2* buf, int nseq, const Geo&, const void* tw, int* ws) {
+    int* ex = ws;
+    int* sh = ws + 4;
+    fx::seq_max_exp(buf, N, nseq, N, ex);
+    if (threadIdx.x < nseq) sh[threadIdx.x] = fx::block_shift(ex[threadIdx.x], G);
+    __syncthreads();
+    fx::seq_to_fixed(buf, N, nseq, N, sh);
+    fx::FPow2Fft<N, 1, INV>::run(reinterpret_cast<longlong2*>(buf), N, nseq,
+                             reinterpret_cast<const longlong2*>(tw), 1);
+    fx::seq_from_fixed(buf, N, nseq, N, sh, 0);
+  }
+};
+
+// shared layout of the column kernels: [tw (ny)] [nseq sequences (ny)] [8 ints]
+__device__ __forceinline__ int* col_ws(double2* sm, int ny, int nseq) {
+  return reinterpret_cast<int*>(sm + (size_t)ny * (1 + nseq));
+}
+
 // generic column FFT over planes: spectral <- mixed (forward, rfft2 2nd half)
 // or mixed <- spectral (inverse, irfft2 1st half)
-template <bool INV>
+template <class CE, bool INV>
 __global__ void k_col_batch(Geo g, const double2* __restrict__ src,
-                            double2* __restrict__ dst) {
+                            double2* __restrict__ dst, const longlong2* __restrict__ twq) {
   extern __shared__ double2 sm[];
   const int ny = g.ny, nk = g.nk;
   const int p = blockIdx.x, k = blockIdx.y;
-  double2* tw = sm;
   double2* b = sm + ny;
-  load_tw(tw, g.twy, ny);
+  CE::load(sm, g, twq);
   for (int l = threadIdx.x; l < ny; l += blockDim.x) b[l] = src[cidx(p, l, k, ny, nk)];
   __syncthreads();
-  fft_run<INV>(b, ny, 1, g.fy, tw, 1);
+  CE::template run<INV>(b, 1, g, sm, col_ws(sm, ny, 1));
   for (int l = threadIdx.x; l < ny; l += blockDim.x) dst[cidx(p, l, k, ny, nk)] = b[l];
 }
 
 // _invert, column part: ph = a qh; uh = -il ph; vh = ik ph (optionally
 // stored); inverse y transforms of uh, vh -> mixed U, V.
+template <class CE>
 __global__ void k_col_invert(Geo g, Consts c, const double2* __restrict__ qh,
                              double2* ph, double2* uh, double2* vh,
-                             double2* mixU, double2* mixV) {
+                             double2* mixU, double2* mixV, const longlong2* __restrict__ twq) {
   extern __shared__ double2 sm[];
   const int ny = g.ny, nk = g.nk, nz = g.nz;
   const int z = blockIdx.x, k = blockIdx.y;
-  double2* tw = sm;
   double2* bU = sm + ny;
   double2* bV = bU + ny;
-  load_tw(tw, g.twy, ny);
+  CE::load(sm, g, twq);
   const double kk = c.kk[k];
   for (int l = threadIdx.x; l < ny; l += blockDim.x) {
     double2 p = make_double2(0.0, 0.0);
@@ -288,7 +329,7 @@ __global__ void k_col_invert(Geo g, Consts c, const double2* __restrict__ qh,
     bV[l] = v;
   }
   __syncthreads();
-  fft_run<true>(bU, ny, 2, g.fy, tw, 1);
+  CE::template run<true>(bU, 2, g, sm, col_ws(sm, ny, 2));
   for (int l = threadIdx.x; l < ny; l += blockDim.x) {
     mixU[cidx(z, l, k, ny, nk)] = bU[l];
     mixV[cidx(z, l, k, ny, nk)] = bV[l];
@@ -297,23 +338,23 @@ __global__ void k_col_invert(Geo g, Consts c, const double2* __restrict__ qh,
 
 // _do_advection, column part: y transforms of mixed UQ, VQ -> uqh, vqh
 // (optionally stored); dqhdt = -(ik uqh + il vqh + ikQy ph).
+template <class CE>
 __global__ void k_col_adv(Geo g, Consts c, const double2* __restrict__ mixUQ,
                           const double2* __restrict__ mixVQ,
                           const double2* __restrict__ ph, double2* uqh,
-                          double2* vqh, double2* dqhdt) {
+                          double2* vqh, double2* dqhdt, const longlong2* __restrict__ twq) {
   extern __shared__ double2 sm[];
   const int ny = g.ny, nk = g.nk;
   const int z = blockIdx.x, k = blockIdx.y;
-  double2* tw = sm;
   double2* bU = sm + ny;
   double2* bV = bU + ny;
-  load_tw(tw, g.twy, ny);
+  CE::load(sm, g, twq);
   for (int l = threadIdx.x; l < ny; l += blockDim.x) {
     bU[l] = mixUQ[cidx(z, l, k, ny, nk)];
     bV[l] = mixVQ[cidx(z, l, k, ny, nk)];
   }
   __syncthreads();
-  fft_run<false>(bU, ny, 2, g.fy, tw, 1);
+  CE::template run<false>(bU, 2, g, sm, col_ws(sm, ny, 2));
   const double kk = c.kk[k], kQy = c.kQy[z * nk + k];
   for (int l = threadIdx.x; l < ny; l += blockDim.x) {
     const size_t o = cidx(z, l, k, ny, nk);
@@ -326,16 +367,16 @@ __global__ void k_col_adv(Geo g, Consts c, const double2* __restrict__ mixUQ,
 
 // _forward_timestep, column part: filtered AB update of qh (stored), optional
 // in-place history shift, inverse y transform of the new qh -> mixed Q.
+template <class CE>
 __global__ void k_col_ab3(Geo g, Consts c, double2* qh,
                           const double2* __restrict__ dq, double2* dqp,
                           double2* dqpp, double c1, double c2, double c3,
-                          int rotate, double2* mixQ) {
+                          int rotate, double2* mixQ, const longlong2* __restrict__ twq) {
   extern __shared__ double2 sm[];
   const int ny = g.ny, nk = g.nk;
   const int z = blockIdx.x, k = blockIdx.y;
-  double2* tw = sm;
   double2* b = sm + ny;
-  load_tw(tw, g.twy, ny);
+  CE::load(sm, g, twq);
   for (int l = threadIdx.x; l < ny; l += blockDim.x) {
     const size_t o = cidx(z, l, k, ny, nk);
     const double2 d = dq[o], p = dqp[o], pp = dqpp[o];
@@ -348,7 +389,7 @@ __global__ void k_col_ab3(Geo g, Consts c, double2* qh,
     b[l] = qn;
   }
   __syncthreads();
-  fft_run<true>(b, ny, 1, g.fy, tw, 1);
+  CE::template run<true>(b, 1, g, sm, col_ws(sm, ny, 1));
   for (int l = threadIdx.x; l < ny; l += blockDim.x) mixQ[cidx(z, l, k, ny, nk)] = b[l];
 }
 
@@ -473,6 +514,301 @@ __global__ void k_col_fused(Geo g, Consts c, FusedColArgs A) {
 }
 
 // ===========================================================================
+// FIXED-POINT ENGINE (power-of-two grids): the same two fused kernels with
+// the transforms in 64-bit block fixed point (pqg_fixed.cuh); all pointwise
+// physics stays FP64.
+// ===========================================================================
+
+// C2R pre-processing in fixed point from a double half spectrum (shift S).
+__device__ __forceinline__ void c2r_pre_fx(const double2* __restrict__ X, longlong2* z, int M, int k,
+                                           const longlong2* __restrict__ twq, int S) {
+  using namespace fx;
+  if (k == 0) {
+    const i64 x0 = to_fixed(X[0].x, S), xm = to_fixed(X[M].x, S);
+    z[0] = make_longlong2(x0 + xm, x0 - xm);
+    return;
+  }
+  const double2 ad = X[k], bd = X[M - k];
+  const longlong2 a = make_longlong2(to_fixed(ad.x, S), to_fixed(ad.y, S));
+  const longlong2 b = make_longlong2(to_fixed(bd.x, S), -to_fixed(bd.y, S));
+  const longlong2 A = fadd(a, b), B = fsub(a, b);
+  const longlong2 D = fcmulc(B, twq[k]);
+  z[k] = make_longlong2(A.x - D.y, A.y + D.x);
+  if (k != M - k) z[M - k] = make_longlong2(A.x + D.y, D.x - A.y);
+}
+
+// R2C post-processing in fixed point, writing the double half spectrum.
+// Interior entries are formed as 2X and converted with one more bit of shift.
+__device__ __forceinline__ void r2c_post_fx(const longlong2* z, double2* __restrict__ X, int M, int k,
+                                            const longlong2* __restrict__ twq, int S) {
+  using namespace fx;
+  if (k == 0) {
+    const longlong2 z0 = z[0];
+    X[0] = make_double2(from_fixed(z0.x + z0.y, S), 0.0);
+    X[M] = make_double2(from_fixed(z0.x - z0.y, S), 0.0);
+    return;
+  }
+  const longlong2 a = z[k], bb = z[M - k];
+  const longlong2 b = make_longlong2(bb.x, -bb.y);
+  const longlong2 A = fadd(a, b), B = fsub(a, b);
+  const longlong2 C = fcmul(B, twq[k]);
+  const int S1 = S == kNanShift ? S : S + 1;
+  X[k] = make_double2(from_fixed(A.x + C.y, S1), from_fixed(A.y - C.x, S1));
+  if (k != M - k) X[M - k] = make_double2(from_fixed(A.x - C.y, S1), from_fixed(-(A.y + C.x), S1));
+}
+
+template <int LOGM>
+__global__ void k_row_adv_fx(Geo g, RowAdvArgs A, const longlong2* __restrict__ twq_g, int log2_nxny) {
+  using namespace fx;
+  constexpr int M = 1 << LOGM;
+  constexpr int G_C2R = LOGM + 4;   // growth: packing (3 bits) + length-M transform
+  constexpr int G_R2C = LOGM + 4;
+  extern __shared__ double2 sm[];
+  const int nk = M + 1, nx = 2 * M;
+  const int nrows = g.nz * g.ny;
+  const int r0 = blockIdx.x * A.rb;
+  const int rb = min(A.rb, nrows - r0);
+  longlong2* tw = reinterpret_cast<longlong2*>(sm);
+  double2* bU = sm + nx;
+  double2* bV = bU + A.rb * M;
+  double2* bQ = bV + A.rb * M;
+  int* ex = reinterpret_cast<int*>(bQ + A.rb * M);
+  int* sh = ex + 3 * A.rb;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twq_g[i];
+  const int nmix = (A.mixU ? 1 : 0) + (A.mixV ? 1 : 0) + (A.mixQ ? 1 : 0);
+  for (int i = threadIdx.x; i < 3 * A.rb; i += blockDim.x) ex[i] = 0;
+  __syncthreads();
+  // block exponents of the mixed half spectra (imaginary parts of k = 0 and
+  // k = M are ignored by the C2R and do not count)
+  for (int t = threadIdx.x; t < nmix * rb * nk; t += blockDim.x) {
+    const int f = t / (rb * nk);
+    const int rem = t - f * rb * nk;
+    const int rr = rem / nk, k = rem - rr * nk;
+    const double2* mix = f == 0 ? A.mixU : (f == 1 ? A.mixV : A.mixQ);
+    const double2 v = mix[(size_t)(r0 + rr) * nk + k];
+    atomicMax(&ex[f * A.rb + rr], (k == 0 || k == M) ? bexp1(v.x) : bexp(v));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * A.rb; i += blockDim.x) sh[i] = block_shift(ex[i], G_C2R);
+  __syncthreads();
+  const int half = M / 2 + 1;
+  for (int t = threadIdx.x; t < 3 * rb * half; t += blockDim.x) {
+    const int f = t / (rb * half);
+    const int rem = t - f * rb * half;
+    const int rr = rem / half, k = rem - rr * half;
+    const int r = r0 + rr;
+    const double2* mix = f == 0 ? A.mixU : (f == 1 ? A.mixV : A.mixQ);
+    const double* phys = f == 0 ? A.physU : (f == 1 ? A.physV : A.physQ);
+    double2* b = (f == 0 ? bU : (f == 1 ? bV : bQ)) + rr * M;
+    if (mix) {
+      c2r_pre_fx(mix + (size_t)r * nk, reinterpret_cast<longlong2*>(b), M, k, tw, sh[f * A.rb + rr]);
+    } else {
+      const double2* row = reinterpret_cast<const double2*>(phys + (size_t)r * nx);
+      if (k < M - k) b[k] = row[k];
+      if (k < M - k && M - 1 - k != k) b[M - 1 - k] = row[M - 1 - k];
+    }
+  }
+  __syncthreads();
+  if (nmix) FPow2Fft<M, 1, true>::run(reinterpret_cast<longlong2*>(bU), M, nmix * A.rb, tw, 2);
+
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    const int r = r0 + rr;
+    const int z = r / g.ny;
+    double2 u = bU[rr * M + m], v = bV[rr * M + m], q = bQ[rr * M + m];
+    if (A.mixU) {
+      const longlong2 f = *reinterpret_cast<const longlong2*>(&bU[rr * M + m]);
+      const int S = sh[rr] == kNanShift ? kNanShift : sh[rr] + log2_nxny;
+      u = make_double2(from_fixed(f.x, S), from_fixed(f.y, S));
+    }
+    if (A.mixV) {
+      const longlong2 f = *reinterpret_cast<const longlong2*>(&bV[rr * M + m]);
+      const int S = sh[A.rb + rr] == kNanShift ? kNanShift : sh[A.rb + rr] + log2_nxny;
+      v = make_double2(from_fixed(f.x, S), from_fixed(f.y, S));
+    }
+    if (A.mixQ) {
+      const longlong2 f = *reinterpret_cast<const longlong2*>(&bQ[rr * M + m]);
+      const int S = sh[2 * A.rb + rr] == kNanShift ? kNanShift : sh[2 * A.rb + rr] + log2_nxny;
+      q = make_double2(from_fixed(f.x, S), from_fixed(f.y, S));
+    }
+    const size_t po = (size_t)r * nx + 2 * m;
+    if (A.outU) *reinterpret_cast<double2*>(A.outU + po) = u;
+    if (A.outV) *reinterpret_cast<double2*>(A.outV + po) = v;
+    if (A.outQ) *reinterpret_cast<double2*>(A.outQ + po) = q;
+    const double ub = A.Ubg[z];
+    const double2 uq = make_double2(__dmul_rn(__dadd_rn(u.x, ub), q.x),
+                                    __dmul_rn(__dadd_rn(u.y, ub), q.y));
+    const double2 vq = make_double2(__dmul_rn(v.x, q.x), __dmul_rn(v.y, q.y));
+    if (A.outUQ) *reinterpret_cast<double2*>(A.outUQ + po) = uq;
+    if (A.outVQ) *reinterpret_cast<double2*>(A.outVQ + po) = vq;
+    bU[rr * M + m] = uq;
+    bV[rr * M + m] = vq;
+  }
+  __syncthreads();
+  seq_max_exp(bU, M, 2 * A.rb, M, ex);
+  for (int i = threadIdx.x; i < 2 * A.rb; i += blockDim.x) sh[i] = block_shift(ex[i], G_R2C);
+  __syncthreads();
+  seq_to_fixed(bU, M, 2 * A.rb, M, sh);
+  FPow2Fft<M, 1, false>::run(reinterpret_cast<longlong2*>(bU), M, 2 * A.rb, tw, 2);
+  for (int t = threadIdx.x; t < 2 * rb * half; t += blockDim.x) {
+    const int f = t / (rb * half);
+    const int rem = t - f * rb * half;
+    const int rr = rem / half, k = rem - rr * half;
+    const int r = r0 + rr;
+    double2* X = (f == 0 ? A.mixUQ : A.mixVQ) + (size_t)r * nk;
+    r2c_post_fx(reinterpret_cast<const longlong2*>((f == 0 ? bU : bV) + rr * M), X, M, k, tw,
+                sh[f * A.rb + rr]);
+  }
+}
+
+// Fixed-point counterparts of k_row_c2r / k_row_r2c: the same block
+// exponent rule, packing and transform as k_row_adv_fx, so that results
+// match the fused kernels bit for bit.
+template <int LOGM>
+__global__ void k_row_c2r_fx(Geo g, RowBatchArgs A, const longlong2* __restrict__ twq_g, int log2_nxny) {
+  using namespace fx;
+  constexpr int M = 1 << LOGM;
+  constexpr int G_C2R = LOGM + 4;
+  extern __shared__ double2 sm[];
+  const int nk = M + 1, nx = 2 * M;
+  const int r0 = blockIdx.x * A.rb;
+  const int rb = min(A.rb, A.nrows - r0);
+  longlong2* tw = reinterpret_cast<longlong2*>(sm);
+  double2* b = sm + nx;
+  int* ex = reinterpret_cast<int*>(b + A.rb * M);
+  int* sh = ex + A.rb;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twq_g[i];
+  for (int i = threadIdx.x; i < A.rb; i += blockDim.x) ex[i] = 0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < rb * nk; t += blockDim.x) {
+    const int rr = t / nk, k = t - rr * nk;
+    const double2 v = A.mixsrc[(size_t)(r0 + rr) * nk + k];
+    atomicMax(&ex[rr], (k == 0 || k == M) ? bexp1(v.x) : bexp(v));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < A.rb; i += blockDim.x) sh[i] = block_shift(ex[i], G_C2R);
+  __syncthreads();
+  const int half = M / 2 + 1;
+  for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
+    const int rr = t / half, k = t - rr * half;
+    c2r_pre_fx(A.mixsrc + (size_t)(r0 + rr) * nk, reinterpret_cast<longlong2*>(b + rr * M), M, k, tw, sh[rr]);
+  }
+  __syncthreads();
+  FPow2Fft<M, 1, true>::run(reinterpret_cast<longlong2*>(b), M, A.rb, tw, 2);
+  for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    const longlong2 f = *reinterpret_cast<const longlong2*>(&b[rr * M + m]);
+    const int S = sh[rr] == kNanShift ? kNanShift : sh[rr] + log2_nxny;
+    *reinterpret_cast<double2*>(A.phys + (size_t)(r0 + rr) * nx + 2 * m) =
+        make_double2(from_fixed(f.x, S), from_fixed(f.y, S));
+  }
+}
+
+template <int LOGM>
+__global__ void k_row_r2c_fx(Geo g, RowBatchArgs A, const longlong2* __restrict__ twq_g) {
+  using namespace fx;
+  constexpr int M = 1 << LOGM;
+  constexpr int G_R2C = LOGM + 4;
+  extern __shared__ double2 sm[];
+  const int nk = M + 1, nx = 2 * M;
+  const int r0 = blockIdx.x * A.rb;
+  const int rb = min(A.rb, A.nrows - r0);
+  longlong2* tw = reinterpret_cast<longlong2*>(sm);
+  double2* b = sm + nx;
+  int* ex = reinterpret_cast<int*>(b + A.rb * M);
+  int* sh = ex + A.rb;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twq_g[i];
+  for (int t = threadIdx.x; t < A.rb * M; t += blockDim.x) {
+    const int rr = t / M, m = t - rr * M;
+    b[rr * M + m] = rr < rb ? reinterpret_cast<const double2*>(A.physsrc + (size_t)(r0 + rr) * nx)[m]
+                            : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  seq_max_exp(b, M, A.rb, M, ex);
+  for (int i = threadIdx.x; i < A.rb; i += blockDim.x) sh[i] = block_shift(ex[i], G_R2C);
+  __syncthreads();
+  seq_to_fixed(b, M, A.rb, M, sh);
+  FPow2Fft<M, 1, false>::run(reinterpret_cast<longlong2*>(b), M, A.rb, tw, 2);
+  const int half = M / 2 + 1;
+  for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
+    const int rr = t / half, k = t - rr * half;
+    r2c_post_fx(reinterpret_cast<const longlong2*>(b + rr * M), A.mixdst + (size_t)(r0 + rr) * nk, M, k,
+                tw, sh[rr]);
+  }
+}
+
+template <int LOGN>
+__global__ void k_col_fused_fx(Geo g, Consts c, FusedColArgs A, const longlong2* __restrict__ twq_g) {
+  using namespace fx;
+  constexpr int N = 1 << LOGN;
+  extern __shared__ double2 sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int ny = N, nk = g.nk, nz = g.nz;
+  const int z = blockIdx.x, k = blockIdx.y;
+  longlong2* tw = reinterpret_cast<longlong2*>(sm);
+  double2* bU = sm + ny;      // UQ, later U
+  double2* bV = bU + ny;      // VQ, later V
+  double2* bQN = bV + ny;     // qh (new) of this layer
+  double2* bQO = bQN + ny;    // qh (old) of this layer
+  int* ex = reinterpret_cast<int*>(bQO + ny);
+  ColFx<LOGN>::load(tw, g, twq_g);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    bU[l] = A.mixUQ[o];
+    bV[l] = A.mixVQ[o];
+    bQO[l] = A.qh[o];
+  }
+  __syncthreads();
+  ColFx<LOGN>::template run<false>(bU, 2, g, tw, ex);
+  cluster.sync();  // qh(old) of every layer is in shared memory
+
+  const double kk = c.kk[k], kQy = c.kQy[z * nk + k];
+  const bool drag = (c.rek != 0.0) && (z == nz - 1);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    double2 p = make_double2(0.0, 0.0);
+    for (int z1 = 0; z1 < nz; z1++) {
+      const double2* rq = cluster.map_shared_rank(bQO, z1);
+      p = ph_acc(p, c.a[cidx(z * nz + z1, l, k, ny, nk)], rq[l]);
+    }
+    const double2 uqh = bU[l], vqh = bV[l];
+    const double ll = c.ll[l];
+    if (A.ph) A.ph[o] = p;
+    if (A.uh) A.uh[o] = uh_of(ll, p);
+    if (A.vh) A.vh[o] = vh_of(kk, p);
+    if (A.uqh) A.uqh[o] = uqh;
+    if (A.vqh) A.vqh[o] = vqh;
+    double2 d = tendency(kk, ll, kQy, uqh, vqh, p);
+    if (drag) d = friction(d, __dmul_rn(c.rek, c.k2l2[(size_t)l * nk + k]), p);
+    if (A.forcing) d = cadd(d, A.forcing[o]);
+    const double2 pv = A.dqp[o], ppv = A.dqpp[o];
+    const double2 qn = ab_update(c.filtr[(size_t)l * nk + k], bQO[l], d, pv, ppv, A.c1, A.c2, A.c3);
+    A.qh[o] = qn;
+    A.dqout[o] = d;
+    bQN[l] = qn;
+  }
+  cluster.sync();  // qh(new) of every layer is in shared memory
+
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    double2 p = make_double2(0.0, 0.0);
+    for (int z1 = 0; z1 < nz; z1++) {
+      const double2* rq = cluster.map_shared_rank(bQN, z1);
+      p = ph_acc(p, c.a[cidx(z * nz + z1, l, k, ny, nk)], rq[l]);
+    }
+    bU[l] = uh_of(c.ll[l], p);
+    bV[l] = vh_of(kk, p);
+  }
+  cluster.sync();  // remote reads of bQN done before it is transformed
+  ColFx<LOGN>::template run<true>(bU, 3, g, tw, ex);
+  for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+    const size_t o = cidx(z, l, k, ny, nk);
+    A.mixU[o] = bU[l];
+    A.mixV[o] = bV[l];
+    A.mixQ[o] = bQN[l];
+  }
+}
+
+// ===========================================================================
 // plan
 // ===========================================================================
 struct GraphEntry {
@@ -497,6 +833,10 @@ struct pqg_plan {
   double rek = 0.0;
   std::vector<double> h_kk, h_ll, h_Qy;
   bool have_kk = false, have_ll = false, have_qy = false;
+  longlong2* twx_q = nullptr;  // Q62 twiddles for the fixed-point engine
+  longlong2* twy_q = nullptr;
+  int engine = 0;              // 0: FP64 transforms, 1: fixed-point transforms
+  int log2_nxny = 0;
   double2* scratch = nullptr;  // mixed planes
   int scratch_planes = 0;
   int T_row = 128, rb = 1, T_col = 256;
@@ -544,30 +884,45 @@ static int min_threads(const FftDesc& d) {
   return t;
 }
 
-// exp(-2 pi i m / n) for m = 0..n-1, accurate to the last bit in practice:
-// angles are folded into [0, pi/4] and evaluated in long double.
+// cos and sin of 2 pi m / n in long double, with the angle folded into
+// [0, pi/4] so that the tables are accurate to the last bit in practice.
+static void cos_sin_ld(int n, int m, long double& cr, long double& sr) {
+  const long double pi = 3.141592653589793238462643383279502884L;
+  long long num = 8LL * m;          // angle = 2 pi m / n = (pi/4) * (8m/n)
+  long long oct = num / n;          // octant 0..7
+  long long rem = num - oct * n;    // angle within octant = (pi/4) rem / n
+  long double x = pi / 4 * (long double)rem / (long double)n;
+  long double c = cosl(x), s = sinl(x);
+  switch (oct) {
+    case 0: cr = c; sr = s; break;
+    case 1: { long double y = pi / 4 - x; cr = sinl(y); sr = cosl(y); break; }
+    case 2: cr = -s; sr = c; break;
+    case 3: { long double y = pi / 4 - x; cr = -cosl(y); sr = sinl(y); break; }
+    case 4: cr = -c; sr = -s; break;
+    case 5: { long double y = pi / 4 - x; cr = -sinl(y); sr = -cosl(y); break; }
+    case 6: cr = s; sr = -c; break;
+    default: { long double y = pi / 4 - x; cr = cosl(y); sr = -sinl(y); break; }
+  }
+}
+
+// exp(-2 pi i m / n) for m = 0..n-1 (FP64 table)
 static void twiddles(int n, std::vector<double2>& w) {
   w.resize(n);
-  const long double pi = 3.141592653589793238462643383279502884L;
   for (int m = 0; m < n; m++) {
-    // reduce 8m/n into an octant index and remainder
-    long long num = 8LL * m;          // angle = 2 pi m / n = (pi/4) * (8m/n)
-    long long oct = num / n;          // octant 0..7
-    long long rem = num - oct * n;    // angle within octant = (pi/4) rem / n
-    long double x = pi / 4 * (long double)rem / (long double)n;
-    long double c = cosl(x), s = sinl(x);
-    long double cr, sr;               // cos, sin of the full angle
-    switch (oct) {
-      case 0: cr = c; sr = s; break;
-      case 1: { long double y = pi / 4 - x; cr = sinl(y); sr = cosl(y); break; }
-      case 2: cr = -s; sr = c; break;
-      case 3: { long double y = pi / 4 - x; cr = -cosl(y); sr = sinl(y); break; }
-      case 4: cr = -c; sr = -s; break;
-      case 5: { long double y = pi / 4 - x; cr = -sinl(y); sr = -cosl(y); break; }
-      case 6: cr = s; sr = -c; break;
-      default: { long double y = pi / 4 - x; cr = cosl(y); sr = -sinl(y); break; }
-    }
+    long double cr, sr;
+    cos_sin_ld(n, m, cr, sr);
     w[m] = make_double2((double)cr, -(double)sr);
+  }
+}
+
+// the same table as Q62 integers (round(2^62 cos), round(-2^62 sin))
+static void twiddles_q62(int n, std::vector<longlong2>& w) {
+  w.resize(n);
+  const long double one = 4611686018427387904.0L;  // 2^62
+  for (int m = 0; m < n; m++) {
+    long double cr, sr;
+    cos_sin_ld(n, m, cr, sr);
+    w[m] = make_longlong2(llroundl(cr * one), llroundl(-sr * one));
   }
 }
 
@@ -578,7 +933,7 @@ static size_t row_batch_smem(const pqg_plan* p, int rb) {
   return sizeof(double2) * ((size_t)p->nx + (size_t)rb * p->M);
 }
 static size_t col_smem(const pqg_plan* p, int nseq) {
-  return sizeof(double2) * ((size_t)p->ny * (1 + nseq));
+  return sizeof(double2) * ((size_t)p->ny * (1 + nseq)) + 8 * sizeof(int);
 }
 
 static Geo geo(const pqg_plan* p) {
@@ -657,6 +1012,101 @@ static ColFusedFn col_fused_kernel(int ny) {
   return k_col_fused<FftRuntime>;
 }
 
+typedef void (*RowAdvFxFn)(Geo, RowAdvArgs, const longlong2*, int);
+typedef void (*ColFusedFxFn)(Geo, Consts, FusedColArgs, const longlong2*);
+
+static RowAdvFxFn row_adv_fx_kernel(int M) {
+  switch (is_pow2(M) ? ilog2(M) : -1) {
+    case 3: return k_row_adv_fx<3>;
+    case 4: return k_row_adv_fx<4>;
+    case 5: return k_row_adv_fx<5>;
+    case 6: return k_row_adv_fx<6>;
+    case 7: return k_row_adv_fx<7>;
+    case 8: return k_row_adv_fx<8>;
+    case 9: return k_row_adv_fx<9>;
+    case 10: return k_row_adv_fx<10>;
+    default: return nullptr;
+  }
+}
+
+static ColFusedFxFn col_fused_fx_kernel(int ny) {
+  switch (is_pow2(ny) ? ilog2(ny) : -1) {
+    case 4: return k_col_fused_fx<4>;
+    case 5: return k_col_fused_fx<5>;
+    case 6: return k_col_fused_fx<6>;
+    case 7: return k_col_fused_fx<7>;
+    case 8: return k_col_fused_fx<8>;
+    case 9: return k_col_fused_fx<9>;
+    case 10: return k_col_fused_fx<10>;
+    default: return nullptr;
+  }
+}
+
+typedef void (*ColBatchFn)(Geo, const double2*, double2*, const longlong2*);
+typedef void (*ColInvertFn)(Geo, Consts, const double2*, double2*, double2*, double2*, double2*, double2*,
+                            const longlong2*);
+typedef void (*ColAdvFn)(Geo, Consts, const double2*, const double2*, const double2*, double2*, double2*,
+                         double2*, const longlong2*);
+typedef void (*ColAb3Fn)(Geo, Consts, double2*, const double2*, double2*, double2*, double, double, double, int,
+                         double2*, const longlong2*);
+typedef void (*RowC2rFxFn)(Geo, RowBatchArgs, const longlong2*, int);
+typedef void (*RowR2cFxFn)(Geo, RowBatchArgs, const longlong2*);
+
+#define PQG_LOGN_CASES(X) X(4) X(5) X(6) X(7) X(8) X(9) X(10)
+#define PQG_LOGM_CASES(X) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10)
+
+// The plan's engine selects every column transform: FP64 with the runtime
+// plan, or fixed point with the compile-time plan of length ny.
+template <bool INV>
+static ColBatchFn col_batch_kernel(int engine, int ny) {
+  if (engine == 1) switch (ilog2(ny)) {
+#define C(L) case L: return k_col_batch<ColFx<L>, INV>;
+      PQG_LOGN_CASES(C)
+#undef C
+    }
+  return k_col_batch<ColRT, INV>;
+}
+static ColInvertFn col_invert_kernel(int engine, int ny) {
+  if (engine == 1) switch (ilog2(ny)) {
+#define C(L) case L: return k_col_invert<ColFx<L>>;
+      PQG_LOGN_CASES(C)
+#undef C
+    }
+  return k_col_invert<ColRT>;
+}
+static ColAdvFn col_adv_kernel(int engine, int ny) {
+  if (engine == 1) switch (ilog2(ny)) {
+#define C(L) case L: return k_col_adv<ColFx<L>>;
+      PQG_LOGN_CASES(C)
+#undef C
+    }
+  return k_col_adv<ColRT>;
+}
+static ColAb3Fn col_ab3_kernel(int engine, int ny) {
+  if (engine == 1) switch (ilog2(ny)) {
+#define C(L) case L: return k_col_ab3<ColFx<L>>;
+      PQG_LOGN_CASES(C)
+#undef C
+    }
+  return k_col_ab3<ColRT>;
+}
+static RowC2rFxFn row_c2r_fx_kernel(int M) {
+  switch (is_pow2(M) ? ilog2(M) : -1) {
+#define C(L) case L: return k_row_c2r_fx<L>;
+    PQG_LOGM_CASES(C)
+#undef C
+    default: return nullptr;
+  }
+}
+static RowR2cFxFn row_r2c_fx_kernel(int M) {
+  switch (is_pow2(M) ? ilog2(M) : -1) {
+#define C(L) case L: return k_row_r2c_fx<L>;
+    PQG_LOGM_CASES(C)
+#undef C
+    default: return nullptr;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // launch helpers (stage kernels)
 // ---------------------------------------------------------------------------
@@ -666,39 +1116,57 @@ static int launch_row_adv(pqg_plan* p, const RowAdvArgs& A0, cudaStream_t st) {
   A.Ubg = p->Ubg;
   const int nrows = p->nz * p->ny;
   const int grid = (nrows + A.rb - 1) / A.rb;
-  row_adv_kernel(p->M)<<<grid, p->T_row, row_adv_smem(p, A.rb), st>>>(geo(p), A);
+  if (p->engine == 1) {
+    const size_t smem = row_adv_smem(p, A.rb) + sizeof(int) * 6 * A.rb;
+    row_adv_fx_kernel(p->M)<<<grid, p->T_row, smem, st>>>(geo(p), A, p->twx_q, p->log2_nxny);
+  } else {
+    row_adv_kernel(p->M)<<<grid, p->T_row, row_adv_smem(p, A.rb), st>>>(geo(p), A);
+  }
   CHECK_LAUNCH();
   return PQG_OK;
 }
 
-static int launch_row_c2r(pqg_plan* p, const double2* mix, double* phys, int nplanes, cudaStream_t st) {
+static int launch_row_c2r(pqg_plan* p, const double2* mix, double* phys, int nplanes, cudaStream_t st,
+                          int engine) {
   RowBatchArgs A{};
   A.mixsrc = mix;
   A.phys = phys;
   A.nrows = nplanes * p->ny;
   A.rb = p->rb_batch;
   const int grid = (A.nrows + A.rb - 1) / A.rb;
-  k_row_c2r<<<grid, p->T_row_batch, row_batch_smem(p, A.rb), st>>>(geo(p), A);
+  if (engine == 1) {
+    const size_t smem = row_batch_smem(p, A.rb) + sizeof(int) * 2 * A.rb;
+    row_c2r_fx_kernel(p->M)<<<grid, p->T_row_batch, smem, st>>>(geo(p), A, p->twx_q, p->log2_nxny);
+  } else {
+    k_row_c2r<<<grid, p->T_row_batch, row_batch_smem(p, A.rb), st>>>(geo(p), A);
+  }
   CHECK_LAUNCH();
   return PQG_OK;
 }
 
-static int launch_row_r2c(pqg_plan* p, const double* phys, double2* mix, int nplanes, cudaStream_t st) {
+static int launch_row_r2c(pqg_plan* p, const double* phys, double2* mix, int nplanes, cudaStream_t st,
+                          int engine) {
   RowBatchArgs A{};
   A.physsrc = phys;
   A.mixdst = mix;
   A.nrows = nplanes * p->ny;
   A.rb = p->rb_batch;
   const int grid = (A.nrows + A.rb - 1) / A.rb;
-  k_row_r2c<<<grid, p->T_row_batch, row_batch_smem(p, A.rb), st>>>(geo(p), A);
+  if (engine == 1) {
+    const size_t smem = row_batch_smem(p, A.rb) + sizeof(int) * 2 * A.rb;
+    row_r2c_fx_kernel(p->M)<<<grid, p->T_row_batch, smem, st>>>(geo(p), A, p->twx_q);
+  } else {
+    k_row_r2c<<<grid, p->T_row_batch, row_batch_smem(p, A.rb), st>>>(geo(p), A);
+  }
   CHECK_LAUNCH();
   return PQG_OK;
 }
 
 template <bool INV>
-static int launch_col_batch(pqg_plan* p, const double2* src, double2* dst, int nplanes, cudaStream_t st) {
+static int launch_col_batch(pqg_plan* p, const double2* src, double2* dst, int nplanes, cudaStream_t st,
+                            int engine) {
   dim3 grid(nplanes, p->nk);
-  k_col_batch<INV><<<grid, p->T_col, col_smem(p, 1), st>>>(geo(p), src, dst);
+  col_batch_kernel<INV>(engine, p->ny)<<<grid, p->T_col, col_smem(p, 1), st>>>(geo(p), src, dst, p->twy_q);
   CHECK_LAUNCH();
   return PQG_OK;
 }
@@ -716,7 +1184,12 @@ static int launch_col_fused(pqg_plan* p, const FusedColArgs& A, cudaStream_t st)
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  PQG_CUDA(cudaLaunchKernelEx(&cfg, col_fused_kernel(p->ny), geo(p), consts(p), A));
+  if (p->engine == 1) {
+    cfg.dynamicSmemBytes = col_smem(p, 4) + sizeof(int) * 8;
+    PQG_CUDA(cudaLaunchKernelEx(&cfg, col_fused_fx_kernel(p->ny), geo(p), consts(p), A, (const longlong2*)p->twy_q));
+  } else {
+    PQG_CUDA(cudaLaunchKernelEx(&cfg, col_fused_kernel(p->ny), geo(p), consts(p), A));
+  }
   return PQG_OK;
 }
 
@@ -736,14 +1209,27 @@ static int set_smem_limits() {
   PQG_CUDA(cudaFuncSetAttribute(row_adv_kernel(3), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(k_row_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PQG_CUDA(cudaFuncSetAttribute(k_col_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PQG_CUDA(cudaFuncSetAttribute(k_col_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PQG_CUDA(cudaFuncSetAttribute(k_col_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PQG_CUDA(cudaFuncSetAttribute(k_col_adv, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PQG_CUDA(cudaFuncSetAttribute(k_col_ab3, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  for (int engine = 0; engine < 2; engine++)
+    for (int n = 16; n <= 1024; n *= 2) {
+      PQG_CUDA(cudaFuncSetAttribute(col_batch_kernel<true>(engine, n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      PQG_CUDA(cudaFuncSetAttribute(col_batch_kernel<false>(engine, n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      PQG_CUDA(cudaFuncSetAttribute(col_invert_kernel(engine, n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      PQG_CUDA(cudaFuncSetAttribute(col_adv_kernel(engine, n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      PQG_CUDA(cudaFuncSetAttribute(col_ab3_kernel(engine, n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    }
+  for (int m = 8; m <= 1024; m *= 2) {
+    PQG_CUDA(cudaFuncSetAttribute(row_c2r_fx_kernel(m), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    PQG_CUDA(cudaFuncSetAttribute(row_r2c_fx_kernel(m), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  }
   for (int n = 16; n <= 1024; n *= 2) {
     PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(n), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  }
+  for (int m = 8; m <= 1024; m *= 2)
+    PQG_CUDA(cudaFuncSetAttribute(row_adv_fx_kernel(m), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  for (int n = 16; n <= 1024; n *= 2) {
+    PQG_CUDA(cudaFuncSetAttribute(col_fused_fx_kernel(n), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    PQG_CUDA(cudaFuncSetAttribute(col_fused_fx_kernel(n), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   }
   PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(3), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(3), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -819,6 +1305,18 @@ PQG_API int pqg_plan_create(pqg_plan** out, int nz, int ny, int nx) {
   cudaMemcpy(p->twx, w.data(), sizeof(double2) * nx, cudaMemcpyHostToDevice);
   twiddles(ny, w);
   cudaMemcpy(p->twy, w.data(), sizeof(double2) * ny, cudaMemcpyHostToDevice);
+  // fixed-point engine: power-of-two grids within the compiled plans
+  if (is_pow2(nx) && is_pow2(ny) && row_adv_fx_kernel(p->M) && col_fused_fx_kernel(ny) &&
+      row_c2r_fx_kernel(p->M) && row_r2c_fx_kernel(p->M)) {
+    std::vector<longlong2> wq;
+    ok = alloc((void**)&p->twx_q, sizeof(longlong2) * nx) && alloc((void**)&p->twy_q, sizeof(longlong2) * ny);
+    if (!ok) { pqg_plan_destroy(p); return fail(PQG_ERR_NOMEM, "cudaMalloc failed in plan_create"); }
+    twiddles_q62(nx, wq);
+    cudaMemcpy(p->twx_q, wq.data(), sizeof(longlong2) * nx, cudaMemcpyHostToDevice);
+    twiddles_q62(ny, wq);
+    cudaMemcpy(p->twy_q, wq.data(), sizeof(longlong2) * ny, cudaMemcpyHostToDevice);
+    p->log2_nxny = ilog2(nx) + ilog2(ny);
+  }
   rc = ensure_scratch(p, 5 * nz);
   if (rc) { pqg_plan_destroy(p); return rc; }
   if (cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -835,7 +1333,7 @@ PQG_API int pqg_plan_destroy(pqg_plan* p) {
   drop_graphs(p);
   cudaFree(p->twx); cudaFree(p->twy); cudaFree(p->a); cudaFree(p->kk);
   cudaFree(p->ll); cudaFree(p->k2l2); cudaFree(p->kQy); cudaFree(p->Ubg);
-  cudaFree(p->filtr); cudaFree(p->scratch);
+  cudaFree(p->filtr); cudaFree(p->scratch); cudaFree(p->twx_q); cudaFree(p->twy_q);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   delete p;
   return PQG_OK;
@@ -909,6 +1407,17 @@ PQG_API int pqg_set_filter(pqg_plan* p, const double* filtr) {
   return upload(p->filtr, filtr, (size_t)p->ny * p->nk);
 }
 
+PQG_API int pqg_set_engine(pqg_plan* p, int engine) {
+  if (!p) return fail(PQG_ERR_INVALID, "NULL argument");
+  if (engine != 0 && engine != 1) return fail(PQG_ERR_INVALID, "engine must be 0 (FP64) or 1 (fixed point)");
+  if (engine == 1 && !p->twx_q) return fail(PQG_ERR_UNSUPPORTED, "the fixed-point engine needs power-of-two nx, ny (16..2048)");
+  if (engine != p->engine) drop_graphs(p);
+  p->engine = engine;
+  return PQG_OK;
+}
+
+PQG_API int pqg_get_engine(const pqg_plan* p) { return p ? p->engine : -1; }
+
 PQG_API int pqg_set_rek(pqg_plan* p, double rek) {
   if (!p) return fail(PQG_ERR_INVALID, "NULL argument");
   if (rek != p->rek) drop_graphs(p);
@@ -923,8 +1432,8 @@ PQG_API int pqg_rfft2(pqg_plan* p, const double* x, double* xh, int nplanes, voi
   const size_t pr = (size_t)p->ny * p->nx, pc = (size_t)p->ny * p->nk;
   for (int p0 = 0; p0 < nplanes; p0 += chunk) {
     const int n = std::min(chunk, nplanes - p0);
-    int rc = launch_row_r2c(p, x + p0 * pr, p->scratch, n, st);
-    if (!rc) rc = launch_col_batch<false>(p, p->scratch, dc(xh) + p0 * pc, n, st);
+    int rc = launch_row_r2c(p, x + p0 * pr, p->scratch, n, st, 0);
+    if (!rc) rc = launch_col_batch<false>(p, p->scratch, dc(xh) + p0 * pc, n, st, 0);
     if (rc) return rc;
   }
   return PQG_OK;
@@ -937,8 +1446,8 @@ PQG_API int pqg_irfft2(pqg_plan* p, const double* xh, double* x, int nplanes, vo
   const size_t pr = (size_t)p->ny * p->nx, pc = (size_t)p->ny * p->nk;
   for (int p0 = 0; p0 < nplanes; p0 += chunk) {
     const int n = std::min(chunk, nplanes - p0);
-    int rc = launch_col_batch<true>(p, dc(xh) + p0 * pc, p->scratch, n, st);
-    if (!rc) rc = launch_row_c2r(p, p->scratch, x + p0 * pr, n, st);
+    int rc = launch_col_batch<true>(p, dc(xh) + p0 * pc, p->scratch, n, st, 0);
+    if (!rc) rc = launch_row_c2r(p, p->scratch, x + p0 * pr, n, st, 0);
     if (rc) return rc;
   }
   return PQG_OK;
@@ -952,10 +1461,10 @@ PQG_API int pqg_invert(pqg_plan* p, const double* qh, double* ph, double* uh, do
   double2* mU = p->scratch;
   double2* mV = p->scratch + p->nz * pc;
   dim3 grid(p->nz, p->nk);
-  k_col_invert<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), dc(qh), dc(ph), dc(uh), dc(vh), mU, mV);
+  col_invert_kernel(p->engine, p->ny)<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), dc(qh), dc(ph), dc(uh), dc(vh), mU, mV, p->twy_q);
   CHECK_LAUNCH();
-  int rc = launch_row_c2r(p, mU, u, p->nz, st);
-  if (!rc) rc = launch_row_c2r(p, mV, v, p->nz, st);
+  int rc = launch_row_c2r(p, mU, u, p->nz, st, p->engine);
+  if (!rc) rc = launch_row_c2r(p, mV, v, p->nz, st, p->engine);
   return rc;
 }
 
@@ -973,7 +1482,7 @@ PQG_API int pqg_do_advection(pqg_plan* p, const double* q, const double* u, cons
   int rc = launch_row_adv(p, A, st);
   if (rc) return rc;
   dim3 grid(p->nz, p->nk);
-  k_col_adv<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), A.mixUQ, A.mixVQ, dc(ph), dc(uqh), dc(vqh), dc(dqhdt));
+  col_adv_kernel(p->engine, p->ny)<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), A.mixUQ, A.mixVQ, dc(ph), dc(uqh), dc(vqh), dc(dqhdt), p->twy_q);
   CHECK_LAUNCH();
   return PQG_OK;
 }
@@ -994,8 +1503,8 @@ PQG_API int pqg_do_q_forcing(pqg_plan* p, const double* dq, double* dqh, double*
   int rc = ensure_scratch(p, 4 * p->nz);
   if (rc) return rc;
   double2* tmp = dqh ? dc(dqh) : p->scratch + 3 * p->nz * pc;
-  rc = launch_row_r2c(p, dq, p->scratch, p->nz, st);
-  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tmp, p->nz, st);
+  rc = launch_row_r2c(p, dq, p->scratch, p->nz, st, p->engine);
+  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tmp, p->nz, st, p->engine);
   if (rc) return rc;
   const size_t n = p->nz * pc;
   k_add_q<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(geo(p), tmp, dc(dqhdt));
@@ -1012,10 +1521,10 @@ PQG_API int pqg_do_uv_forcing(pqg_plan* p, const double* du, const double* dv, d
   if (rc) return rc;
   double2* tu = duh ? dc(duh) : p->scratch + 3 * p->nz * pc;
   double2* tv = dvh ? dc(dvh) : p->scratch + 4 * p->nz * pc;
-  rc = launch_row_r2c(p, du, p->scratch, p->nz, st);
-  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tu, p->nz, st);
-  if (!rc) rc = launch_row_r2c(p, dv, p->scratch, p->nz, st);
-  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tv, p->nz, st);
+  rc = launch_row_r2c(p, du, p->scratch, p->nz, st, p->engine);
+  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tu, p->nz, st, p->engine);
+  if (!rc) rc = launch_row_r2c(p, dv, p->scratch, p->nz, st, p->engine);
+  if (!rc) rc = launch_col_batch<false>(p, p->scratch, tv, p->nz, st, p->engine);
   if (rc) return rc;
   const size_t n = p->nz * pc;
   k_add_uv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(geo(p), consts(p), tu, tv, dc(dqhdt));
@@ -1031,10 +1540,10 @@ PQG_API int pqg_forward_timestep(pqg_plan* p, int ablevel, double dt, double* qh
   double c1, c2, c3;
   ab_coeffs(ablevel, dt, c1, c2, c3);
   dim3 grid(p->nz, p->nk);
-  k_col_ab3<<<grid, p->T_col, col_smem(p, 1), st>>>(geo(p), consts(p), dc(qh), dc(dqhdt), dc(dqhdt_p),
-                                                     dc(dqhdt_pp), c1, c2, c3, rotate, p->scratch);
+  col_ab3_kernel(p->engine, p->ny)<<<grid, p->T_col, col_smem(p, 1), st>>>(
+      geo(p), consts(p), dc(qh), dc(dqhdt), dc(dqhdt_p), dc(dqhdt_pp), c1, c2, c3, rotate, p->scratch, p->twy_q);
   CHECK_LAUNCH();
-  return launch_row_c2r(p, p->scratch, q, p->nz, st);
+  return launch_row_c2r(p, p->scratch, q, p->nz, st, p->engine);
 }
 
 // one fused step: row kernel (+ column kernel); `first` reads physical q.
@@ -1087,8 +1596,8 @@ PQG_API int pqg_step(pqg_plan* p, pqg_state* s, int nsteps, const pqg_aux* aux, 
   const size_t pc = (size_t)p->ny * p->nk;
   // prologue: mixed U, V of the current qh
   dim3 grid(p->nz, p->nk);
-  k_col_invert<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), dc(s->qh), nullptr, nullptr, nullptr,
-                                                        p->scratch, p->scratch + p->nz * pc);
+  col_invert_kernel(p->engine, p->ny)<<<grid, p->T_col, col_smem(p, 2), st>>>(
+      geo(p), consts(p), dc(s->qh), nullptr, nullptr, nullptr, p->scratch, p->scratch + p->nz * pc, p->twy_q);
   CHECK_LAUNCH();
   int done = 0;
   int rc = fused_step(p, s, true, nsteps == 1 ? aux : nullptr, st);
@@ -1156,7 +1665,7 @@ PQG_API int pqg_step(pqg_plan* p, pqg_state* s, int nsteps, const pqg_aux* aux, 
     done++;
   }
   // epilogue: physical q of the final state
-  return launch_row_c2r(p, p->scratch + 2 * p->nz * pc, s->q, p->nz, st);
+  return launch_row_c2r(p, p->scratch + 2 * p->nz * pc, s->q, p->nz, st, p->engine);
 }
 
 PQG_API int pqg_step_profile(pqg_plan* p, pqg_state* s, int nsteps, double* ms, int* counts,
@@ -1166,14 +1675,14 @@ PQG_API int pqg_step_profile(pqg_plan* p, pqg_state* s, int nsteps, double* ms, 
   cudaStream_t st = (cudaStream_t)stream;
   const size_t pc = (size_t)p->ny * p->nk;
   dim3 grid(p->nz, p->nk);
-  k_col_invert<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), dc(s->qh), nullptr, nullptr, nullptr,
-                                                        p->scratch, p->scratch + p->nz * pc);
+  col_invert_kernel(p->engine, p->ny)<<<grid, p->T_col, col_smem(p, 2), st>>>(
+      geo(p), consts(p), dc(s->qh), nullptr, nullptr, nullptr, p->scratch, p->scratch + p->nz * pc, p->twy_q);
   CHECK_LAUNCH();
   std::vector<cudaEvent_t> ev(3 * nsteps);
   for (auto& e : ev) PQG_CUDA(cudaEventCreate(&e));
   int rc = PQG_OK;
   for (int i = 0; i < nsteps && !rc; i++) rc = fused_step(p, s, i == 0, nullptr, st, &ev[3 * i]);
-  if (!rc) rc = launch_row_c2r(p, p->scratch + 2 * p->nz * pc, s->q, p->nz, st);
+  if (!rc) rc = launch_row_c2r(p, p->scratch + 2 * p->nz * pc, s->q, p->nz, st, p->engine);
   if (!rc) {
     PQG_CUDA(cudaStreamSynchronize(st));
     ms[0] = ms[1] = 0.0;
@@ -1286,8 +1795,8 @@ PQG_API int pqg_rfft2_noalloc(const double* x, double* xh, int nplanes, int ny, 
     p.twy = d.twy;
     p.scratch = d.scratch;
   }
-  rc = launch_row_r2c(&p, x, p.scratch, nplanes, st);
-  if (!rc) rc = launch_col_batch<false>(&p, p.scratch, reinterpret_cast<double2*>(xh), nplanes, st);
+  rc = launch_row_r2c(&p, x, p.scratch, nplanes, st, 0);
+  if (!rc) rc = launch_col_batch<false>(&p, p.scratch, reinterpret_cast<double2*>(xh), nplanes, st, 0);
   p.twx = p.twy = nullptr;  // not owned: keep the plan destructor-free path
   p.scratch = nullptr;
   return rc;

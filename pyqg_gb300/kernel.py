@@ -21,6 +21,7 @@ a role that shares its buffer with another is given a free buffer before it
 is written (copy-on-write).
 """
 import ctypes
+import os
 
 import numpy as np
 import torch
@@ -31,6 +32,11 @@ _PHYS = ("q", "u", "v", "uq", "vq", "dq", "du", "dv")
 _SPEC = ("qh", "ph", "uh", "vh", "uqh", "vqh", "dqh", "duh", "dvh")
 _TEND = ("dqhdt", "dqhdt_p", "dqhdt_pp")
 _AUX = ("ph", "uh", "vh", "u", "v", "uq", "vq", "uqh", "vqh")
+
+# Transform engine of the fused step for new kernels: "fixed" (64-bit block
+# fixed point, used where the grid allows it) or "fp64".  PQG_ENGINE
+# overrides it.
+DEFAULT_ENGINE = os.environ.get("PQG_ENGINE", "fixed")
 
 
 def _check_array(x, dtype, ndim, name):
@@ -71,6 +77,9 @@ class PseudoSpectralKernel:
         plan = ctypes.c_void_p()
         _lib.check(L.pqg_plan_create(ctypes.byref(plan), self.nz, self.ny, self.nx))
         self._plan = plan
+        self._engine = "fp64"
+        if DEFAULT_ENGINE == "fixed" and L.pqg_set_engine(plan, 1) == _lib.PQG_OK:
+            self._engine = "fixed"
         dev = self._device
         shp_r = (self.nz, self.ny, self.nx)
         shp_c = (self.nz, self.nl, self.nk)
@@ -128,6 +137,19 @@ class PseudoSpectralKernel:
             except Exception:
                 pass
             self.__dict__["_plan"] = None
+
+    @property
+    def engine(self):
+        """Transform engine of the fused step: 'fixed' (64-bit block fixed
+        point, the default on power-of-two grids) or 'fp64'."""
+        return self._engine
+
+    @engine.setter
+    def engine(self, name):
+        if name not in ("fixed", "fp64"):
+            raise ValueError("engine must be 'fixed' or 'fp64'")
+        _lib.check(self._L.pqg_set_engine(self._plan, 1 if name == "fixed" else 0))
+        self._engine = name
 
     # ------------------------------------------------------------------
     # buffer plumbing
@@ -552,6 +574,41 @@ class PseudoSpectralKernel:
     @property
     def vfull(self):
         return self._get("v")
+
+    # -- checkpoint / exact resume ------------------------------------------
+    def save_checkpoint(self, path):
+        """Write the complete time-stepping state to `path` (.npz): q, qh,
+        the three tendencies, ablevel, t, tc, dt.  Loading it into a model
+        built with the same parameters resumes the run bit for bit (the
+        reference's snapshot output drops the Adams-Bashforth history)."""
+        state = dict(q=self._get("q").copy(), qh=self._get("qh").copy(),
+                     dqhdt=self._get("dqhdt").copy(),
+                     dqhdt_p=self._get("dqhdt_p").copy(),
+                     dqhdt_pp=self._get("dqhdt_pp").copy(),
+                     ablevel=np.int64(self._ablevel), t=np.float64(self._t),
+                     tc=np.int64(self._tc), dt=np.float64(self._dt),
+                     shape=np.array([self.nz, self.ny, self.nx]),
+                     engine=np.array(self._engine))
+        np.savez(path, **state)
+
+    def load_checkpoint(self, path):
+        """Restore a state written by :meth:`save_checkpoint`."""
+        with np.load(path, allow_pickle=False) as f:
+            st = {k: f[k] for k in f.files}
+        if tuple(st["shape"]) != (self.nz, self.ny, self.nx):
+            raise ValueError("checkpoint grid %s does not match this model %s"
+                             % (tuple(st["shape"]), (self.nz, self.ny, self.nx)))
+        self._sync_in()
+        self._role = {"dqhdt": 0, "dqhdt_p": 1, "dqhdt_pp": 2}
+        for name in ("q", "qh", "dqhdt", "dqhdt_p", "dqhdt_pp"):
+            self._upload(name, st[name])
+        self._stream.synchronize()
+        self._dt = float(st["dt"])
+        self._ablevel = int(st["ablevel"])
+        self._t = float(st["t"])
+        self._tc = int(st["tc"])
+        if str(st["engine"]) != self._engine:
+            self.engine = str(st["engine"])
 
     # -- device views (no host copy): for GPU-side parameterizations -------
     def device_field(self, name):

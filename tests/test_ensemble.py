@@ -1,0 +1,108 @@
+"""Batched ensembles: FP64 members reproduce the single-model FP64 step bit
+for bit; members are independent of their group; the FP32 form's error
+against the FP64 oracle; FP64 energy and enstrophy sums."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+QUIET = dict(tavestart=1e30, taveint=1e30, log_level=0)
+
+
+def _qg(seed_beta, rek, nx=64, dt=7200.0):
+    return ("qg", dict(nx=nx, dt=dt, beta=seed_beta, rek=rek))
+
+
+def test_fp64_members_equal_single_models():
+    import pyqg_gb300 as P
+    specs = [_qg(1.5e-11, 5.787e-7), _qg(2.1e-11, 3.0e-7), _qg(0.9e-11, 9.0e-7)]
+    rng = np.random.default_rng(0)
+    q0 = [1e-7 * rng.standard_normal((2, 64, 64)) for _ in specs]
+    ens = P.Ensemble(specs, precision="fp64")
+    ens.set_q(q0)
+    ens.step(50)
+    for i, (kind, kw) in enumerate(specs):
+        m = P.QGModel(nx=64, dt=7200.0, beta=kw["beta"], rek=kw["rek"], tmax=50 * 7200.0, **QUIET)
+        m.engine = "fp64"
+        m.q = q0[i]
+        m.run()
+        np.testing.assert_array_equal(ens.q(i), m.q)
+
+
+def test_members_are_independent_of_their_group():
+    import pyqg_gb300 as P
+    rng = np.random.default_rng(1)
+    specs = [_qg(1.5e-11 * (1 + 0.1 * i), 5.787e-7) for i in range(5)]
+    q0 = [1e-7 * rng.standard_normal((2, 64, 64)) for _ in specs]
+    big = P.Ensemble(specs, precision="fp32")
+    big.set_q(q0)
+    big.step(30)
+    alone = P.Ensemble([specs[3]], precision="fp32")
+    alone.set_q([q0[3]])
+    alone.step(30)
+    np.testing.assert_array_equal(big.q(3), alone.q(0))
+
+
+def test_uneven_sizes_and_layered_members():
+    import pyqg_gb300 as P
+    rng = np.random.default_rng(2)
+    lay = dict(nz=3, H=[500., 1000., 2500.], U=[0.05, 0.02, 0.0], V=[0., 0., 0.])
+    specs = [_qg(1.5e-11, 5.787e-7, nx=32), _qg(1.5e-11, 5.787e-7, nx=64),
+             ("layered", dict(nx=64, dt=7200.0, **lay)), _qg(1.5e-11, 5.787e-7, nx=128)]
+    q0 = []
+    for kind, kw in specs:
+        nz = 3 if kind == "layered" else 2
+        q0.append(1e-7 * rng.standard_normal((nz, kw["nx"], kw["nx"])))
+    ens = P.Ensemble(specs, precision="fp64")
+    assert len(ens.groups) == 4
+    ens.set_q(q0)
+    ens.step(20)
+    # the layered member against the single-model FP64 step
+    m = P.LayeredModel(nx=64, dt=7200.0, tmax=20 * 7200.0, **lay, **QUIET)
+    m.engine = "fp64"
+    m.q = q0[2]
+    m.run()
+    np.testing.assert_array_equal(ens.q(2), m.q)
+    ke, en = ens.energy()
+    assert all(np.all(np.isfinite(k)) and np.all(k > 0) for k in ke)
+
+
+def test_energy_sums_match_host_fp64():
+    import pyqg_gb300 as P
+    rng = np.random.default_rng(4)
+    q0 = 1e-7 * rng.standard_normal((2, 64, 64))
+    ens = P.Ensemble([_qg(1.5e-11, 5.787e-7)], precision="fp64")
+    ens.set_q([q0])
+    ens.step(10)
+    ke, en = ens.energy()
+    m = P.QGModel(nx=64, dt=7200.0, tmax=10 * 7200.0, **QUIET)
+    m.engine = "fp64"
+    m.q = q0
+    m.run()
+    m._invert()
+    for z in range(2):
+        np.testing.assert_allclose(ke[0][z], 0.5 * m.spec_var(m.wv * m.ph[z]), rtol=1e-12)
+        np.testing.assert_allclose(en[0][z], 0.5 * m.spec_var(m.qh[z]), rtol=1e-12)
+
+
+def test_fp32_form_error_vs_fp64_oracle():
+    """FP32 state, transforms, products and AB3 (FP64-built matrices): the
+    10-step pointwise relative L2 error on q against the FP64 oracle."""
+    import pyqg_gb300 as P
+    import pyqg_oracle as O
+    rng = np.random.default_rng(5)
+    q0 = 1e-7 * rng.standard_normal((2, 256, 256))
+    ens = P.Ensemble([_qg(1.5e-11, 5.787e-7, nx=256, dt=3600.0)], precision="fp32")
+    ens.set_q([q0])
+    ens.step(10)
+    c = O.qg_constants(256)
+    o = O.OracleKernel(2, 256, 256, c["a"], c["kk"], c["ll"], c["Ubg"], c["Qy"], c["filtr"],
+                       5.787e-7, 3600.0)
+    o.set_q(q0)
+    for _ in range(10):
+        o.step()
+    err = rel_l2(ens.q(0), o.q)
+    print("FP32 form, nx=256, 10 steps: relative L2 error on q = %.3e" % err)
+    assert err < 1e-5

@@ -94,11 +94,13 @@ def test_100_steps_config1(P, quiet):
     assert rel_l2(m.q, g["q_100"]) < TOL_100
 
 
-def test_fused_is_bit_identical_to_staged(P, quiet):
+@pytest.mark.parametrize("engine", ["fp64", "fixed"])
+def test_fused_is_bit_identical_to_staged(P, quiet, engine):
     rng = np.random.default_rng(5)
     q0 = 1e-7 * rng.standard_normal((2, 64, 64))
     a = P.QGModel(nx=64, dt=7200.0, **C1, **quiet)
     b = P.QGModel(nx=64, dt=7200.0, **C1, **quiet)
+    a.engine = b.engine = engine
     a.q = q0
     b.q = q0
     for _ in range(40):
@@ -187,3 +189,56 @@ def test_layered_fixture_inversion(P):
     m._invert()
     assert rel_l2(m.ph, g["ph"]) < TOL_STAGE
     assert rel_l2(m.u, g["u"]) < TOL_STAGE
+
+
+@pytest.mark.parametrize("engine", ["fp64", "fixed"])
+def test_engines_100_steps(P, quiet, engine):
+    """Both transform engines of the fused step pass the 1e-12 gate, at
+    config-1 (vs the reference) and config-2 (vs the oracle) physics."""
+    import pyqg_oracle as O
+    g = golden("qg_c1_nx64.npz")
+    m = P.QGModel(nx=64, dt=7200.0, tmax=100 * 7200.0, **C1, **quiet)
+    m.engine = engine
+    m.q = g["q0"]
+    m.run()
+    assert rel_l2(m.q, g["q_100"]) < TOL_100
+    q0 = 1e-7 * np.random.default_rng(1).standard_normal((2, 256, 256))
+    m = P.QGModel(nx=256, dt=3600.0, tmax=100 * 3600.0, **C1, **quiet)
+    m.engine = engine
+    m.q = q0
+    m.run()
+    o = O.OracleKernel(2, 256, 256, m.a.real, m.kk, m.ll, m.Ubg, m.Qy, m.filtr, m.rek, m.dt)
+    o.set_q(q0)
+    for _ in range(100):
+        o.step()
+    assert rel_l2(m.q, o.q) < TOL_100
+
+
+def test_fixed_engine_extreme_magnitudes(P, quiet):
+    """Block exponents follow the data: fields from 1e-150 to the largest
+    amplitude the dynamics survives step like the FP64 engine, and a zero
+    field stays exactly zero."""
+    rng = np.random.default_rng(9)
+    m = P.QGModel(nx=64, dt=7200.0, tmax=5 * 7200.0, **C1, **quiet)
+    m.engine = "fixed"
+    m.q = np.zeros((2, 64, 64))
+    m.run()
+    assert not np.any(m.q)
+    for scale in (1e-150, 1e-7, 1e-6):
+        q0 = scale * rng.standard_normal((2, 64, 64))
+        res = {}
+        for engine in ("fp64", "fixed"):
+            m = P.QGModel(nx=64, dt=7200.0, tmax=20 * 7200.0, **C1, **quiet)
+            m.engine = engine
+            m.q = q0
+            m.run()
+            res[engine] = m.q.copy()
+        assert np.all(np.isfinite(res["fixed"]))
+        assert rel_l2(res["fixed"], res["fp64"]) < 1e-13
+
+
+def test_fixed_engine_unavailable_on_odd_sizes(P, quiet):
+    m = P.QGModel(nx=96, **quiet)
+    assert m.engine == "fp64"
+    with pytest.raises(NotImplementedError):
+        m.engine = "fixed"
