@@ -189,7 +189,9 @@ int pqg_ens_step_many(pqg_ens **ens, int count, int nsteps, void *stream);
 /* FP64 sums per (member, layer): ke = 0.5 sum |kappa ph|^2 / M^2 and
  * enstrophy 0.5 sum |qh|^2 / M^2 over the full spectral plane (host out) */
 int pqg_ens_energy(pqg_ens *ens, double *ke, double *enstrophy, void *stream);
-/* device pointers of the state (q, qh) and the step counter / time */
+/* device pointers of the state and the step counter / time: q is
+ * (B, nz, ny, nx) and qh is (B, nz, nk, ny) -- column-contiguous, the
+ * transpose of the single-model layout -- both in the ensemble precision */
 int pqg_ens_state(pqg_ens *ens, void **q, void **qh, long long *tc,
                   double *t);
 

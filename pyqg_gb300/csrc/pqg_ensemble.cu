@@ -82,82 +82,76 @@ struct EGeo {
 
 template <class S>
 struct EConsts {
-  const S* a;      // (nz, nz, ny, nk)
+  const S* a;      // (nz, nz, nk, ny)  column-major in (l, k)
   const S* kk;     // (nk)
   const S* ll;     // (ny)
-  const S* k2l2;   // (ny, nk)
-  const S* filtr;  // (ny, nk)
+  const S* k2l2;   // (nk, ny)
+  const S* filtr;  // (nk, ny)
   const S* kQy;    // (B, nz, nk)
   const S* Ubg;    // (B, nz)
   const S* rek;    // (B)
 };
 
+// Ensemble layout, k-major so that a spectral column is contiguous:
+// spectral (B, nz, nk, ny); scratch plane (f, z) of member b holds the mixed
+// values (k, y) at b*mstride + (f*nz + z)*ny*nk + k*ny + y.
 __device__ __forceinline__ size_t sidx(int b, int z, int l, int k, int nz, int ny, int nk) {
-  return (((size_t)b * nz + z) * ny + l) * nk + k;
+  return (((size_t)b * nz + z) * nk + k) * ny + l;
 }
 
 // ---------------------------------------------------------------------------
-// row kernel: rows of all members; C2R of mixed U, V and Q (or physical q),
-// products, R2C of uq, vq back into the U, V planes
+// row kernel: rows of all members (rb consecutive rows of one plane per CTA);
+// C2R of mixed U, V and Q (or physical q), products, R2C of uq, vq back into
+// the U, V planes.  Spectral values of a row are at stride ny.
 // ---------------------------------------------------------------------------
 template <class V, int LOGM>
 __global__ void e_row_adv(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, const typename Sc<V>::T* qphys,
-                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb_) {
+                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb) {
   typedef typename Sc<V>::T S;
   constexpr int M = 1 << LOGM;
   extern __shared__ __align__(16) unsigned char esm[];
   V* tw = reinterpret_cast<V*>(esm);
-  const int nk = M + 1, nx = 2 * M;
-  const int rows_m = g.nz * g.ny;
-  const int nrows = g.B * rows_m;
-  const int r0 = blockIdx.x * rb_;
-  const int rb = min(rb_, nrows - r0);
+  const int nx = 2 * M, ny = g.ny;
+  const int rows_m = g.nz * ny;
+  const int r0 = blockIdx.x * rb;            // rb divides ny: one plane per CTA
+  const int b = r0 / rows_m, rm = r0 - b * rows_m;
+  const int z = rm / ny, y0 = rm - z * ny;
+  const size_t plane = (size_t)ny * g.nk;
+  V* base = scratch + b * g.mstride + (size_t)z * plane + y0;   // field 0 (U)
   V* bU = tw + nx;
-  V* bV = bU + rb_ * M;
-  V* bQ = bV + rb_ * M;
+  V* bV = bU + rb * M;
+  V* bQ = bV + rb * M;
   for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
   __syncthreads();
   const int half = M / 2 + 1;
-  const size_t plane3 = (size_t)g.nz * g.ny * nk;
   for (int t = threadIdx.x; t < 3 * rb * half; t += blockDim.x) {
-    const int f = t / (rb * half);
-    const int rem = t - f * rb * half;
-    const int rr = rem / half, k = rem - rr * half;
-    const int r = r0 + rr;
-    const int b = r / rows_m, rm = r - b * rows_m;
+    const int rr = t % rb, rest = t / rb;
+    const int k = rest % half, f = rest / half;
     V* buf = (f == 0 ? bU : (f == 1 ? bV : bQ)) + rr * M;
     if (f < 2 || !qphys) {
-      const V* X = scratch + b * g.mstride + f * plane3 + (size_t)rm * nk;
-      c2r_pre(X, buf, M, k, tw);
+      c2r_pre_s(base + (size_t)f * g.nz * plane + rr, ny, buf, M, k, tw);
     } else {
-      const V* row = reinterpret_cast<const V*>(qphys + (size_t)r * nx);
+      const V* row = reinterpret_cast<const V*>(qphys + (size_t)(r0 + rr) * nx);
       if (k < M - k) buf[k] = row[k];
       if (k < M - k && M - 1 - k != k) buf[M - 1 - k] = row[M - 1 - k];
     }
   }
   __syncthreads();
-  Pow2Fft<M, 1, true, V>::run(bU, M, (qphys ? 2 : 3) * rb_, tw, 2);
+  Pow2Fft<M, 1, true, V>::run(bU, M, (qphys ? 2 : 3) * rb, tw, 2);
+  const S ub = c.Ubg[b * g.nz + z];
   for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
-    const int rr = t / M, m = t - rr * M;
-    const int r = r0 + rr;
-    const int b = r / rows_m, z = (r - b * rows_m) / g.ny;
-    V u = cscale(bU[rr * M + m], scale), v = cscale(bV[rr * M + m], scale);
-    V q = bQ[rr * M + m];
+    V u = cscale(bU[t], scale), v = cscale(bV[t], scale);
+    V q = bQ[t];
     if (!qphys) q = cscale(q, scale);
-    const S ub = c.Ubg[b * g.nz + z];
-    bU[rr * M + m] = mk(smul(sadd(u.x, ub), q.x), smul(sadd(u.y, ub), q.y));
-    bV[rr * M + m] = mk(smul(v.x, q.x), smul(v.y, q.y));
+    bU[t] = mk(smul(sadd(u.x, ub), q.x), smul(sadd(u.y, ub), q.y));
+    bV[t] = mk(smul(v.x, q.x), smul(v.y, q.y));
   }
   __syncthreads();
-  Pow2Fft<M, 1, false, V>::run(bU, M, 2 * rb_, tw, 2);
+  Pow2Fft<M, 1, false, V>::run(bU, M, 2 * rb, tw, 2);
   for (int t = threadIdx.x; t < 2 * rb * half; t += blockDim.x) {
-    const int f = t / (rb * half);
-    const int rem = t - f * rb * half;
-    const int rr = rem / half, k = rem - rr * half;
-    const int r = r0 + rr;
-    const int b = r / rows_m, rm = r - b * rows_m;
-    V* X = scratch + b * g.mstride + f * plane3 + (size_t)rm * nk;
-    r2c_post((f == 0 ? bU : bV) + rr * M, X, M, k, tw);
+    const int rr = t % rb, rest = t / rb;
+    const int k = rest % half, f = rest / half;
+    r2c_post_s((f == 0 ? bU : bV) + rr * M, base + (size_t)f * g.nz * plane + rr, ny, M, k, tw);
   }
 }
 
@@ -187,11 +181,12 @@ __global__ void e_col_fused(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, V*
   V* mQ = mV + (size_t)nz * plane;
   for (int i = threadIdx.x; i < ny; i += blockDim.x) tw[i] = twy[i];
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
     const bool ok = k < nk;
-    bU[cc * ny + l] = ok ? mU[(size_t)l * nk + k] : mk((S)0, (S)0);
-    bV[cc * ny + l] = ok ? mV[(size_t)l * nk + k] : mk((S)0, (S)0);
-    bQO[cc * ny + l] = ok ? qh[sidx(b, z, l, k, nz, ny, nk)] : mk((S)0, (S)0);
+    const size_t mo = (size_t)k * ny + l;
+    bU[t] = ok ? mU[mo] : mk((S)0, (S)0);
+    bV[t] = ok ? mV[mo] : mk((S)0, (S)0);
+    bQO[t] = ok ? qh[sidx(b, z, l, k, nz, ny, nk)] : mk((S)0, (S)0);
   }
   __syncthreads();
   Pow2Fft<N, 1, false, V>::run(bU, ny, 2 * C, tw, 1);
@@ -199,46 +194,46 @@ __global__ void e_col_fused(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, V*
   const S rek = c.rek[b];
   const bool drag = (rek != (S)0) && (z == nz - 1);
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
     if (k >= nk) continue;
-    const int i = cc * ny + l;
     const size_t o = sidx(b, z, l, k, nz, ny, nk);
+    const size_t ck = (size_t)k * ny + l;
     V p = mk((S)0, (S)0);
     for (int z1 = 0; z1 < nz; z1++) {
       const V* rq = cluster.map_shared_rank(bQO, z1);
-      p = g_ph_acc(p, c.a[(((size_t)z * nz + z1) * ny + l) * nk + k], rq[i]);
+      p = g_ph_acc(p, c.a[((size_t)z * nz + z1) * plane + ck], rq[t]);
     }
     const S kk = c.kk[k], kQy = c.kQy[((size_t)b * nz + z) * nk + k];
-    V d = g_tendency(kk, c.ll[l], kQy, bU[i], bV[i], p);
-    if (drag) d = g_friction(d, smul(rek, c.k2l2[(size_t)l * nk + k]), p);
+    V d = g_tendency(kk, c.ll[l], kQy, bU[t], bV[t], p);
+    if (drag) d = g_friction(d, smul(rek, c.k2l2[ck]), p);
     const V pv = dqp[o], ppv = dqpp[o];
-    const V qn = g_ab(c.filtr[(size_t)l * nk + k], bQO[i], d, pv, ppv, c1, c2, c3);
+    const V qn = g_ab(c.filtr[ck], bQO[t], d, pv, ppv, c1, c2, c3);
     qh[o] = qn;
     dqpp[o] = d;   // the newest tendency takes the oldest one's buffer
-    bQN[i] = qn;
+    bQN[t] = qn;
   }
   cluster.sync();
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
-    const int i = cc * ny + l;
-    if (k >= nk) { bU[i] = mk((S)0, (S)0); bV[i] = mk((S)0, (S)0); bQN[i] = mk((S)0, (S)0); continue; }
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
+    if (k >= nk) { bU[t] = mk((S)0, (S)0); bV[t] = mk((S)0, (S)0); bQN[t] = mk((S)0, (S)0); continue; }
+    const size_t ck = (size_t)k * ny + l;
     V p = mk((S)0, (S)0);
     for (int z1 = 0; z1 < nz; z1++) {
       const V* rq = cluster.map_shared_rank(bQN, z1);
-      p = g_ph_acc(p, c.a[(((size_t)z * nz + z1) * ny + l) * nk + k], rq[i]);
+      p = g_ph_acc(p, c.a[((size_t)z * nz + z1) * plane + ck], rq[t]);
     }
-    bU[i] = g_uh(c.ll[l], p);
-    bV[i] = g_vh(c.kk[k], p);
+    bU[t] = g_uh(c.ll[l], p);
+    bV[t] = g_vh(c.kk[k], p);
   }
   cluster.sync();
   Pow2Fft<N, 1, true, V>::run(bU, ny, 3 * C, tw, 1);
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
     if (k >= nk) continue;
-    const int i = cc * ny + l;
-    mU[(size_t)l * nk + k] = bU[i];
-    mV[(size_t)l * nk + k] = bV[i];
-    mQ[(size_t)l * nk + k] = bQN[i];
+    const size_t mo = (size_t)k * ny + l;
+    mU[mo] = bU[t];
+    mV[mo] = bV[t];
+    mQ[mo] = bQN[t];
   }
 }
 
@@ -259,77 +254,76 @@ __global__ void e_col_invert(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, c
   V* mV = mU + (size_t)nz * plane;
   for (int i = threadIdx.x; i < ny; i += blockDim.x) tw[i] = twy[i];
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
-    const int i = cc * ny + l;
-    if (k >= nk) { bU[i] = mk((S)0, (S)0); bV[i] = mk((S)0, (S)0); continue; }
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
+    if (k >= nk) { bU[t] = mk((S)0, (S)0); bV[t] = mk((S)0, (S)0); continue; }
+    const size_t ck = (size_t)k * ny + l;
     V p = mk((S)0, (S)0);
     for (int z1 = 0; z1 < nz; z1++)
-      p = g_ph_acc(p, c.a[(((size_t)z * nz + z1) * ny + l) * nk + k], qh[sidx(b, z1, l, k, nz, ny, nk)]);
-    bU[i] = g_uh(c.ll[l], p);
-    bV[i] = g_vh(c.kk[k], p);
+      p = g_ph_acc(p, c.a[((size_t)z * nz + z1) * plane + ck], qh[sidx(b, z1, l, k, nz, ny, nk)]);
+    bU[t] = g_uh(c.ll[l], p);
+    bV[t] = g_vh(c.kk[k], p);
   }
   __syncthreads();
   Pow2Fft<N, 1, true, V>::run(bU, ny, 2 * C, tw, 1);
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
     if (k >= nk) continue;
-    mU[(size_t)l * nk + k] = bU[cc * ny + l];
-    mV[(size_t)l * nk + k] = bV[cc * ny + l];
+    mU[(size_t)k * ny + l] = bU[t];
+    mV[(size_t)k * ny + l] = bV[t];
   }
 }
 
 // mixed plane `field` of every member -> physical (B, nz, ny, nx)
 template <class V, int LOGM>
 __global__ void e_row_c2r(EGeo g, const V* scratch, int field, typename Sc<V>::T* phys,
-                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb_) {
+                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb) {
   constexpr int M = 1 << LOGM;
   extern __shared__ __align__(16) unsigned char esm[];
   V* tw = reinterpret_cast<V*>(esm);
   V* bq = tw + 2 * M;
-  const int nk = M + 1, nx = 2 * M;
-  const int rows_m = g.nz * g.ny, nrows = g.B * rows_m;
-  const int r0 = blockIdx.x * rb_;
-  const int rb = min(rb_, nrows - r0);
+  const int nx = 2 * M, ny = g.ny, rows_m = g.nz * ny;
+  const int r0 = blockIdx.x * rb;
+  const int b = r0 / rows_m, rm = r0 - b * rows_m, z = rm / ny, y0 = rm - z * ny;
+  const size_t plane = (size_t)ny * g.nk;
+  const V* base = scratch + b * g.mstride + ((size_t)field * g.nz + z) * plane + y0;
   for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
   __syncthreads();
   const int half = M / 2 + 1;
-  const size_t plane3 = (size_t)g.nz * g.ny * nk;
   for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
-    const int rr = t / half, k = t - rr * half;
-    const int r = r0 + rr, b = r / rows_m, rm = r - b * rows_m;
-    c2r_pre(scratch + b * g.mstride + field * plane3 + (size_t)rm * nk, bq + rr * M, M, k, tw);
+    const int rr = t % rb, k = t / rb;
+    c2r_pre_s(base + rr, ny, bq + rr * M, M, k, tw);
   }
   __syncthreads();
-  Pow2Fft<M, 1, true, V>::run(bq, M, rb_, tw, 2);
+  Pow2Fft<M, 1, true, V>::run(bq, M, rb, tw, 2);
   for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
     const int rr = t / M, m = t - rr * M;
-    *reinterpret_cast<V*>(phys + (size_t)(r0 + rr) * nx + 2 * m) = cscale(bq[rr * M + m], scale);
+    *reinterpret_cast<V*>(phys + (size_t)(r0 + rr) * nx + 2 * m) = cscale(bq[t], scale);
   }
 }
 
 // physical (B, nz, ny, nx) -> mixed plane 0 of every member
 template <class V, int LOGM>
-__global__ void e_row_r2c(EGeo g, V* scratch, const typename Sc<V>::T* phys, const V* __restrict__ twx, int rb_) {
+__global__ void e_row_r2c(EGeo g, V* scratch, const typename Sc<V>::T* phys, const V* __restrict__ twx, int rb) {
   constexpr int M = 1 << LOGM;
   extern __shared__ __align__(16) unsigned char esm[];
   V* tw = reinterpret_cast<V*>(esm);
   V* bq = tw + 2 * M;
-  const int nk = M + 1, nx = 2 * M;
-  const int rows_m = g.nz * g.ny, nrows = g.B * rows_m;
-  const int r0 = blockIdx.x * rb_;
-  const int rb = min(rb_, nrows - r0);
+  const int nx = 2 * M, ny = g.ny, rows_m = g.nz * ny;
+  const int r0 = blockIdx.x * rb;
+  const int b = r0 / rows_m, rm = r0 - b * rows_m, z = rm / ny, y0 = rm - z * ny;
+  const size_t plane = (size_t)ny * g.nk;
+  V* base = scratch + b * g.mstride + (size_t)z * plane + y0;
   for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
   for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
     const int rr = t / M, m = t - rr * M;
-    bq[rr * M + m] = reinterpret_cast<const V*>(phys + (size_t)(r0 + rr) * nx)[m];
+    bq[t] = reinterpret_cast<const V*>(phys + (size_t)(r0 + rr) * nx)[m];
   }
   __syncthreads();
-  Pow2Fft<M, 1, false, V>::run(bq, M, rb_, tw, 2);
+  Pow2Fft<M, 1, false, V>::run(bq, M, rb, tw, 2);
   const int half = M / 2 + 1;
   for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
-    const int rr = t / half, k = t - rr * half;
-    const int r = r0 + rr, b = r / rows_m, rm = r - b * rows_m;
-    r2c_post(bq + rr * M, scratch + b * g.mstride + (size_t)rm * nk, M, k, tw);
+    const int rr = t % rb, k = t / rb;
+    r2c_post_s(bq + rr * M, base + rr, ny, M, k, tw);
   }
 }
 
@@ -346,14 +340,14 @@ __global__ void e_col_fwd(EGeo g, const V* scratch, V* qh, const V* __restrict__
   const V* m0 = scratch + b * g.mstride + (size_t)z * ny * nk;
   for (int i = threadIdx.x; i < ny; i += blockDim.x) tw[i] = twy[i];
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
-    bq[cc * ny + l] = k < nk ? m0[(size_t)l * nk + k] : mk((S)0, (S)0);
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
+    bq[t] = k < nk ? m0[(size_t)k * ny + l] : mk((S)0, (S)0);
   }
   __syncthreads();
   Pow2Fft<N, 1, false, V>::run(bq, ny, C, tw, 1);
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
-    const int l = t / C, cc = t - l * C, k = k0 + cc;
-    if (k < nk) qh[sidx(b, z, l, k, nz, ny, nk)] = bq[cc * ny + l];
+    const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
+    if (k < nk) qh[sidx(b, z, l, k, nz, ny, nk)] = bq[t];
   }
 }
 
@@ -379,17 +373,17 @@ __global__ void e_energy(EGeo g, EConsts<typename Sc<V>::T> c, const V* qh, doub
   const int nz = g.nz, ny = g.ny, nk = g.nk;
   double ske = 0.0, sen = 0.0;
   for (int i = threadIdx.x; i < ny * nk; i += blockDim.x) {
-    const int l = i / nk, k = i - l * nk;
+    const int k = i / ny, l = i - k * ny;
     double pr = 0.0, pi = 0.0;
     for (int z1 = 0; z1 < nz; z1++) {
-      const double a = (double)c.a[(((size_t)z * nz + z1) * ny + l) * nk + k];
+      const double a = (double)c.a[((size_t)z * nz + z1) * ny * nk + (size_t)k * ny + l];
       const V q = qh[sidx(b, z1, l, k, nz, ny, nk)];
       pr = fma(a, (double)q.x, pr);
       pi = fma(a, (double)q.y, pi);
     }
     const V q = qh[sidx(b, z, l, k, nz, ny, nk)];
     const double w = (k == 0 || k == nk - 1) ? 1.0 : 2.0;
-    const double k2 = (double)c.k2l2[(size_t)l * nk + k];
+    const double k2 = (double)c.k2l2[(size_t)k * ny + l];
     ske += w * k2 * (pr * pr + pi * pi);
     sen += w * ((double)q.x * (double)q.x + (double)q.y * (double)q.y);
   }
@@ -680,13 +674,14 @@ PQG_API int pqg_ens_create(pqg_ens** out, int nmembers, int nz, int ny, int nx, 
   pqg_ens* e = new pqg_ens();
   e->B = nmembers; e->nz = nz; e->ny = ny; e->nx = nx; e->nk = nx / 2 + 1; e->M = nx / 2;
   e->prec = precision; e->esz = precision;
-  e->rb = std::max(1, std::min(16, 256 / e->M));
+  e->rb = std::max(1, std::min(std::min(16, ny), 256 / e->M));   // divides ny (powers of two)
   e->T_row = std::max(64, std::min(256, e->rb * e->M / 2));
   e->C = std::max(1, std::min(8, 512 / ny));
   e->T_col = std::max(64, std::min(256, ny * e->C / 2));
   if (const char* s = getenv("PQG_ENS_C")) e->C = atoi(s);
   if (const char* s = getenv("PQG_ENS_T_ROW")) e->T_row = atoi(s);
-  if (const char* s = getenv("PQG_ENS_RB")) e->rb = atoi(s);
+  if (const char* s = getenv("PQG_ENS_RB")) e->rb = std::max(1, std::min(ny, atoi(s)));
+  if (ny % e->rb) { delete e; return efail(PQG_ERR_INVALID, "rows per block must divide ny"); }
   if (const char* s = getenv("PQG_ENS_T_COL")) e->T_col = atoi(s);
   const size_t S = (size_t)nmembers * nz * ny * e->nk, P = (size_t)nmembers * nz * ny * nx;
   const size_t V = 2 * e->esz;
@@ -725,17 +720,25 @@ PQG_API int pqg_ens_destroy(pqg_ens* e) {
 PQG_API int pqg_ens_set_constants(pqg_ens* e, const double* a, const double* kk, const double* ll,
                                   const double* filtr, double dt) {
   if (!e || !a || !kk || !ll || !filtr) return efail(PQG_ERR_INVALID, "NULL argument");
-  const int nk = e->nk, ny = e->ny;
-  int rc = upload_scalars(e, e->a, a, (size_t)e->nz * e->nz * ny * nk);
+  const int nk = e->nk, ny = e->ny, nz = e->nz;
+  // device copies are k-major: (.., nk, ny)
+  std::vector<double> at((size_t)nz * nz * ny * nk), ft((size_t)ny * nk);
+  for (int zz = 0; zz < nz * nz; zz++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nk; i++)
+        at[(size_t)zz * ny * nk + (size_t)i * ny + j] = a[(size_t)zz * ny * nk + (size_t)j * nk + i];
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nk; i++) ft[(size_t)i * ny + j] = filtr[(size_t)j * nk + i];
+  int rc = upload_scalars(e, e->a, at.data(), at.size());
   if (!rc) rc = upload_scalars(e, e->kk, kk, nk);
   if (!rc) rc = upload_scalars(e, e->ll, ll, ny);
-  if (!rc) rc = upload_scalars(e, e->filtr, filtr, (size_t)ny * nk);
+  if (!rc) rc = upload_scalars(e, e->filtr, ft.data(), ft.size());
   if (rc) return rc;
   std::vector<double> k2l2((size_t)ny * nk);
   for (int j = 0; j < ny; j++)
     for (int i = 0; i < nk; i++) {
       const double x = kk[i] * kk[i], y = ll[j] * ll[j];
-      k2l2[(size_t)j * nk + i] = x + y;
+      k2l2[(size_t)i * ny + j] = x + y;
     }
   rc = upload_scalars(e, e->k2l2, k2l2.data(), k2l2.size());
   if (rc) return rc;

@@ -344,6 +344,44 @@ __device__ __forceinline__ void r2c_post(const V* z,
     X[M - k] = mk(smul(half, ssub(A.x, C.y)), smul(-half, sadd(A.y, C.x)));
 }
 
+// The same packing with the half spectrum at stride `sx` (X[k * sx]), for
+// layouts where a row's spectral values are not contiguous.
+template <class V>
+__device__ __forceinline__ void c2r_pre_s(const V* __restrict__ X, int sx, V* z, int M, int k,
+                                          const V* __restrict__ tw) {
+  if (k == 0) {
+    const auto x0 = X[0].x, xm = X[(size_t)M * sx].x;
+    z[0] = mk(sadd(x0, xm), ssub(x0, xm));
+    return;
+  }
+  const V a = X[(size_t)k * sx], bb = X[(size_t)(M - k) * sx];
+  const V b = mk(bb.x, -bb.y);
+  const V A = cadd(a, b), B = csub(a, b);
+  const V D = cmulc(B, tw[k]);
+  z[k] = mk(ssub(A.x, D.y), sadd(A.y, D.x));
+  if (k != M - k) z[M - k] = mk(sadd(A.x, D.y), ssub(D.x, A.y));
+}
+
+template <class V>
+__device__ __forceinline__ void r2c_post_s(const V* z, V* __restrict__ X, int sx, int M, int k,
+                                           const V* __restrict__ tw) {
+  typedef decltype(z[0].x) S;
+  const S half = (S)0.5;
+  if (k == 0) {
+    const V z0 = z[0];
+    X[0] = mk(sadd(z0.x, z0.y), (S)0);
+    X[(size_t)M * sx] = mk(ssub(z0.x, z0.y), (S)0);
+    return;
+  }
+  const V a = z[k], bb = z[M - k];
+  const V b = mk(bb.x, -bb.y);
+  const V A = cadd(a, b), B = csub(a, b);
+  const V C = cmul(B, tw[k]);
+  X[(size_t)k * sx] = mk(smul(half, sadd(A.x, C.y)), smul(half, ssub(A.y, C.x)));
+  if (k != M - k)
+    X[(size_t)(M - k) * sx] = mk(smul(half, ssub(A.x, C.y)), smul(-half, sadd(A.y, C.x)));
+}
+
 // ---------------------------------------------------------------------------
 // pointwise physics (reference expressions, evaluated with fused
 // multiply-adds; complex products with purely real / imaginary factors
