@@ -34,6 +34,7 @@ extern "C" {
 #define PQG_ERR_CUDA 3         /* CUDA runtime error (message has details)   */
 #define PQG_ERR_NOMEM 4        /* device or host allocation failed           */
 #define PQG_ERR_STATE 5        /* call out of order (e.g. constants unset)   */
+#define PQG_ERR_TIMEOUT 6      /* a bounded device-side wait ran out        */
 
 typedef struct pqg_plan pqg_plan;
 
@@ -221,6 +222,48 @@ int pqg_step_profile(pqg_plan *plan, pqg_state *state, int nsteps,
 #define PQG_NOALLOC_MAX_COMPLEX (1 << 19)
 int pqg_rfft2_noalloc(const double *x, double *xh, int nplanes, int ny,
                       int nx, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Learned subgrid closure (no counterpart in the reference): a fully
+ * convolutional network of 5x5 periodic convolutions with ReLU between
+ * layers, BF16 weights and activations, FP32 accumulation on the tcgen05
+ * tensor cores, trained with Adam.  It reaches a model through the
+ * q_parameterization hook (pyqg/model.py:203-212, pyqg/kernel.pyx:424-442).
+ *
+ * Parameters are one FP32 vector: for each layer, weights w[co][ky][kx][ci]
+ * followed by biases b[co].  Image arrays are NCHW (batch, channels, ny,
+ * nx) device arrays; nx must be 64 and batch * ny * nx a multiple of 128;
+ * hidden channel counts are multiples of 8, all counts at most 128.
+ * --------------------------------------------------------------------- */
+typedef struct pqg_cnn pqg_cnn;
+const char *pqg_cnn_last_error(void);
+/* channels: nlayers + 1 counts (input, hidden..., output) */
+int pqg_cnn_create(pqg_cnn **net, int nlayers, const int *channels, int ny,
+                   int nx, int max_batch);
+int pqg_cnn_destroy(pqg_cnn *net);
+int pqg_cnn_nparams(pqg_cnn *net, long long *n);
+/* host parameter vector in / out (set also resets the Adam moments) */
+int pqg_cnn_set_params(pqg_cnn *net, const float *params, void *stream);
+int pqg_cnn_get_params(pqg_cnn *net, float *params, void *stream);
+int pqg_cnn_get_grads(pqg_cnn *net, float *grads, void *stream);
+/* per-channel standardisation used by pqg_cnn_forward (host arrays) */
+int pqg_cnn_set_norm(pqg_cnn *net, const float *in_mean, const float *in_std,
+                     const float *out_mean, const float *out_std);
+/* y = net((x - in_mean) / in_std) * out_std + out_mean; x and y are FP32
+ * (flag 0) or FP64 (flag 1) device arrays */
+int pqg_cnn_forward(pqg_cnn *net, const void *x, int x_f64, void *y,
+                    int y_f64, int batch, void *stream);
+/* gradient of the mean squared error of net(x) against t (standardised FP32
+ * device arrays) into the gradient vector; the loss before the update is
+ * written to *loss (host) if loss is not NULL */
+int pqg_cnn_backward(pqg_cnn *net, const float *x, const float *t, int batch,
+                     float *loss, void *stream);
+/* one Adam update from the gradient vector */
+int pqg_cnn_adam(pqg_cnn *net, float lr, float beta1, float beta2, float eps,
+                 void *stream);
+/* backward + Adam (beta1 0.9, beta2 0.999, eps 1e-8) */
+int pqg_cnn_train_step(pqg_cnn *net, const float *x, const float *t,
+                       int batch, float lr, float *loss, void *stream);
 
 #ifdef __cplusplus
 }

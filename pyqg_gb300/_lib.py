@@ -16,6 +16,7 @@ PQG_ERR_UNSUPPORTED = 2
 PQG_ERR_CUDA = 3
 PQG_ERR_NOMEM = 4
 PQG_ERR_STATE = 5
+PQG_ERR_TIMEOUT = 6
 
 _P = ctypes.c_void_p
 _D = ctypes.c_double
@@ -73,6 +74,19 @@ SIGNATURES = {
     "pqg_ens_energy": (_I, [_P, _P, _P, _P]),
     "pqg_ens_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
                            ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_D)]),
+    "pqg_cnn_last_error": (ctypes.c_char_p, []),
+    "pqg_cnn_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _I, _I]),
+    "pqg_cnn_destroy": (_I, [_P]),
+    "pqg_cnn_nparams": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
+    "pqg_cnn_set_params": (_I, [_P, _P, _P]),
+    "pqg_cnn_get_params": (_I, [_P, _P, _P]),
+    "pqg_cnn_get_grads": (_I, [_P, _P, _P]),
+    "pqg_cnn_set_norm": (_I, [_P, _P, _P, _P, _P]),
+    "pqg_cnn_forward": (_I, [_P, _P, _I, _P, _I, _I, _P]),
+    "pqg_cnn_backward": (_I, [_P, _P, _P, _I, _P, _P]),
+    "pqg_cnn_adam": (_I, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, _P]),
+    "pqg_cnn_train_step": (_I, [_P, _P, _P, _I, ctypes.c_float, _P, _P]),
 }
 
 _lock = threading.Lock()

@@ -1,0 +1,157 @@
+"""The learned closure's tensor-core convolutions against a PyTorch FP32
+reference of the same network (BF16-rounded weights, inputs and hidden
+activations, circular padding), its gradients against autograd, Adam, and
+the q_parameterization plug-in."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch_net(channels, params, slices, x, round_hidden=True):
+    import torch
+    import torch.nn.functional as F
+    h = x.to(torch.bfloat16).float()
+    nl = len(channels) - 1
+    for i, (ws, shape, bs) in enumerate(slices):
+        w = torch.from_numpy(params[ws].reshape(shape)).cuda().permute(0, 3, 1, 2).contiguous()
+        w = w.to(torch.bfloat16).float()
+        b = torch.from_numpy(params[bs]).cuda()
+        h = F.conv2d(F.pad(h, (2, 2, 2, 2), mode="circular"), w, b)
+        if i < nl - 1:
+            h = torch.relu(h)
+            if round_hidden:
+                h = h.to(torch.bfloat16).float()
+    return h
+
+
+def _reference_grads(channels, params, slices, x, t):
+    import torch
+    import torch.nn.functional as F
+    ws_t = []
+    h = x.to(torch.bfloat16).float()
+    nl = len(channels) - 1
+    for i, (ws, shape, bs) in enumerate(slices):
+        w = torch.from_numpy(params[ws].reshape(shape)).cuda().permute(0, 3, 1, 2).contiguous()
+        w = w.to(torch.bfloat16).float().requires_grad_(True)
+        b = torch.from_numpy(params[bs]).cuda().requires_grad_(True)
+        ws_t.append((w, b))
+        h = F.conv2d(F.pad(h, (2, 2, 2, 2), mode="circular"), w, b)
+        if i < nl - 1:
+            h = torch.relu(h)
+    loss = ((h - t) ** 2).mean()
+    loss.backward()
+    out = []
+    for w, b in ws_t:
+        out.append((w.grad.permute(0, 2, 3, 1).contiguous().cpu().numpy(), b.grad.cpu().numpy()))
+    return float(loss.detach()), out
+
+
+@pytest.mark.parametrize("channels,batch", [((2, 16, 8, 2), 2), ((2, 128, 64, 32, 32, 32, 32, 32, 2), 4)])
+def test_forward_matches_torch(channels, batch):
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    net = ConvNet(channels, max_batch=batch, seed=3)
+    p = net.params
+    rng = np.random.default_rng(0)
+    p += (0.05 * rng.standard_normal(p.shape)).astype(np.float32)  # nonzero biases too
+    net.params = p
+    x = torch.from_numpy(rng.standard_normal((batch, channels[0], 64, 64)).astype(np.float32)).cuda()
+    y = net.forward(x)
+    torch.cuda.synchronize()
+    ref = _torch_net(channels, p, net.layer_slices(), x)
+    err = rel_l2(y.cpu().numpy(), ref.cpu().numpy())
+    assert err < 1e-2, err
+    # FP64 in / out through the same kernels
+    y64 = net.forward(x.double())
+    assert y64.dtype == torch.float64
+    assert rel_l2(y64.cpu().numpy(), y.cpu().numpy()) < 1e-6
+
+
+def test_forward_standardisation():
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    net = ConvNet((2, 16, 2), max_batch=1, seed=1)
+    rng = np.random.default_rng(5)
+    x = torch.from_numpy(rng.standard_normal((1, 2, 64, 64))).cuda()
+    y0 = net.forward(x).cpu().numpy()
+    net.set_norm([0.5, -1.0], [2.0, 4.0], [3.0, -2.0], [10.0, 0.5])
+    xs = x.clone()
+    xs[:, 0] = x[:, 0] * 2.0 + 0.5
+    xs[:, 1] = x[:, 1] * 4.0 - 1.0
+    y1 = net.forward(xs).cpu().numpy()
+    expect = np.stack([y0[:, 0] * 10.0 + 3.0, y0[:, 1] * 0.5 - 2.0], axis=1)
+    assert rel_l2(y1, expect) < 1e-2
+
+
+@pytest.mark.parametrize("channels,batch", [((2, 16, 8, 2), 2), ((2, 128, 64, 32, 32, 32, 32, 32, 2), 2)])
+def test_gradients_match_autograd(channels, batch):
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    net = ConvNet(channels, max_batch=batch, seed=4)
+    p = net.params
+    rng = np.random.default_rng(1)
+    p += (0.02 * rng.standard_normal(p.shape)).astype(np.float32)
+    net.params = p
+    x = torch.from_numpy(rng.standard_normal((batch, channels[0], 64, 64)).astype(np.float32)).cuda()
+    t = torch.from_numpy(rng.standard_normal((batch, channels[-1], 64, 64)).astype(np.float32)).cuda()
+    loss = net.backward(x, t)
+    g = net.grads
+    ref_loss, ref = _reference_grads(channels, p, net.layer_slices(), x, t)
+    assert abs(loss - ref_loss) / ref_loss < 1e-2
+    for (ws, shape, bs), (gw, gb) in zip(net.layer_slices(), ref):
+        assert rel_l2(g[ws].reshape(shape), gw) < 5e-2
+        assert rel_l2(g[bs], gb) < 5e-2
+
+
+def test_adam_reduces_loss():
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    net = ConvNet((2, 32, 32, 2), max_batch=4, seed=2)
+    rng = np.random.default_rng(2)
+    x = torch.from_numpy(rng.standard_normal((4, 2, 64, 64)).astype(np.float32)).cuda()
+    # a target the net can represent: a fixed smoothing of the input
+    t = 0.5 * (x + torch.roll(x, 1, dims=2) + torch.roll(x, -1, dims=3)) / 1.5
+    losses = [net.train_step(x, t, lr=3e-3) for _ in range(60)]
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
+
+
+def test_adam_update_matches_formula():
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    net = ConvNet((2, 16, 2), max_batch=1, seed=6)
+    rng = np.random.default_rng(3)
+    x = torch.from_numpy(rng.standard_normal((1, 2, 64, 64)).astype(np.float32)).cuda()
+    t = torch.from_numpy(rng.standard_normal((1, 2, 64, 64)).astype(np.float32)).cuda()
+    p0 = net.params
+    net.backward(x, t)
+    g = net.grads
+    net.adam(lr=1e-2)
+    p1 = net.params
+    # first Adam step: m_hat = g, v_hat = g^2 -> step = lr * g / (|g| + eps)
+    expect = p0 - 1e-2 * g / (np.abs(g) + 1e-8)
+    np.testing.assert_allclose(p1, expect, rtol=1e-5, atol=1e-6)
+
+
+def test_cnn_parameterization_in_model(quiet):
+    import torch
+    import pyqg_gb300 as P
+    from pyqg_gb300.closure import ConvNet, CNNParameterization
+    net = ConvNet(max_batch=1, seed=7)
+    stats = ([0.0, 0.0], [1e-6, 1e-7], [0.0, 0.0], [1e-12, 1e-13])
+    param = CNNParameterization(net, stats)
+    m = P.QGModel(nx=64, dt=7200.0, q_parameterization=param, **quiet)
+    rng = np.random.default_rng(0)
+    m.q = 1e-7 * rng.standard_normal((2, 64, 64))
+    q_dev = m.device_field("q").clone()
+    dq = param(m)
+    assert isinstance(dq, torch.Tensor) and dq.dtype == torch.float64 and dq.shape == (2, 64, 64)
+    direct = net.forward(q_dev)
+    assert torch.equal(dq, direct)
+    for _ in range(5):
+        m._step_forward()
+    assert np.all(np.isfinite(m.q))
+    assert m.tc == 5
