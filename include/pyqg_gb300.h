@@ -190,6 +190,14 @@ int pqg_ens_step_many(pqg_ens **ens, int count, int nsteps, void *stream);
 /* FP64 sums per (member, layer): ke = 0.5 sum |kappa ph|^2 / M^2 and
  * enstrophy 0.5 sum |qh|^2 / M^2 over the full spectral plane (host out) */
 int pqg_ens_energy(pqg_ens *ens, double *ke, double *enstrophy, void *stream);
+/* learned closure for every member: each step adds the spectral transform
+ * of net(q) to dq/dt after the bottom drag (the q_parameterization hook of
+ * the single-model step).  The network's input and output channels must be
+ * nz, its image (ny, nx) and its batch capacity at least the member count.
+ * NULL detaches.  The ensemble keeps the pointer: destroy the network
+ * after the ensemble or after detaching it.  Synchronizes the device. */
+typedef struct pqg_cnn pqg_cnn;
+int pqg_ens_set_closure(pqg_ens *ens, pqg_cnn *net);
 /* device pointers of the state and the step counter / time: q is
  * (B, nz, ny, nx) and qh is (B, nz, nk, ny) -- column-contiguous, the
  * transpose of the single-model layout -- both in the ensemble precision */
@@ -223,6 +231,22 @@ int pqg_step_profile(pqg_plan *plan, pqg_state *state, int nsteps,
 int pqg_rfft2_noalloc(const double *x, double *xh, int nplanes, int ny,
                       int nx, void *stream);
 
+/* Spectral advective tendency of nplanes physical fields f by (u, v):
+ * out_h = ik fft(u f) + il fft(v f), FP64 transforms
+ * (replaces Model._advect, pyqg/model.py:539-558). */
+int pqg_advect(pqg_plan *plan, const double *f, const double *u,
+               const double *v, int nplanes, double *out_h, void *stream);
+
+/* Coarse-graining of one state (no counterpart in the reference): the fine
+ * spectral PV qh_f (nz, ny_f, nx_f/2+1) is truncated sharply to the coarse
+ * plan's grid (|k| < nx_c/2, |l| < ny_c/2, amplitudes kept) giving q_c
+ * (nz, ny_c, nx_c), and the subgrid forcing
+ *   S = filtered(J(psi, q)) - J(filtered psi, filtered q)
+ * with J(psi, q) = u q_x + v q_y evaluated spectrally on each grid.  Both
+ * plans need their wavenumbers and inversion matrices; FP64 transforms. */
+int pqg_coarse_forcing(pqg_plan *fine, pqg_plan *coarse, const double *qh_f,
+                       double *q_c, double *S, void *stream);
+
 /* ---------------------------------------------------------------------
  * Learned subgrid closure (no counterpart in the reference): a fully
  * convolutional network of 5x5 periodic convolutions with ReLU between
@@ -235,13 +259,15 @@ int pqg_rfft2_noalloc(const double *x, double *xh, int nplanes, int ny,
  * nx) device arrays; nx must be 64 and batch * ny * nx a multiple of 128;
  * hidden channel counts are multiples of 8, all counts at most 128.
  * --------------------------------------------------------------------- */
-typedef struct pqg_cnn pqg_cnn;
 const char *pqg_cnn_last_error(void);
 /* channels: nlayers + 1 counts (input, hidden..., output) */
 int pqg_cnn_create(pqg_cnn **net, int nlayers, const int *channels, int ny,
                    int nx, int max_batch);
 int pqg_cnn_destroy(pqg_cnn *net);
 int pqg_cnn_nparams(pqg_cnn *net, long long *n);
+/* input / output channels, image size and batch capacity (any may be NULL) */
+int pqg_cnn_shape(pqg_cnn *net, int *cin, int *cout, int *ny, int *nx,
+                  int *max_batch);
 /* host parameter vector in / out (set also resets the Adam moments) */
 int pqg_cnn_set_params(pqg_cnn *net, const float *params, void *stream);
 int pqg_cnn_get_params(pqg_cnn *net, float *params, void *stream);

@@ -72,12 +72,16 @@ SIGNATURES = {
     "pqg_ens_step": (_I, [_P, _I, _P]),
     "pqg_ens_step_many": (_I, [ctypes.POINTER(_P), _I, _I, _P]),
     "pqg_ens_energy": (_I, [_P, _P, _P, _P]),
+    "pqg_ens_set_closure": (_I, [_P, _P]),
     "pqg_ens_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
                            ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_D)]),
+    "pqg_advect": (_I, [_P, _P, _P, _P, _I, _P, _P]),
+    "pqg_coarse_forcing": (_I, [_P, _P, _P, _P, _P, _P]),
     "pqg_cnn_last_error": (ctypes.c_char_p, []),
     "pqg_cnn_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _I, _I]),
     "pqg_cnn_destroy": (_I, [_P]),
     "pqg_cnn_nparams": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
+    "pqg_cnn_shape": (_I, [_P] + [ctypes.POINTER(_I)] * 5),
     "pqg_cnn_set_params": (_I, [_P, _P, _P]),
     "pqg_cnn_get_params": (_I, [_P, _P, _P]),
     "pqg_cnn_get_grads": (_I, [_P, _P, _P]),

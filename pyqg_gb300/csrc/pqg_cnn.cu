@@ -512,13 +512,8 @@ int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int
   a.err = net->err;
   const size_t smem = conv_smem(a.N);
   const dim3 grid(a.npix / TM);
-  if (a.cin % 8 == 0) {
-    CCUDA(cudaFuncSetAttribute(k_conv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_conv<true><<<grid, TM, smem, st>>>(a);
-  } else {
-    CCUDA(cudaFuncSetAttribute(k_conv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_conv<false><<<grid, TM, smem, st>>>(a);
-  }
+  if (a.cin % 8 == 0) k_conv<true><<<grid, TM, smem, st>>>(a);
+  else k_conv<false><<<grid, TM, smem, st>>>(a);
   CCUDA(cudaGetLastError());
   return PQG_OK;
 }
@@ -544,17 +539,25 @@ int launch_wgrad(pqg_cnn* net, const CnnLayer& l, const bf16* x, const bf16* g, 
   const size_t smem = conv_smem(a.N);
   const dim3 grid(mt, ks);
   const bool vx = l.cin % 8 == 0, vg = l.cout % 8 == 0;
-#define WG(X, G)                                                                                    \
-  do {                                                                                              \
-    CCUDA(cudaFuncSetAttribute(k_wgrad<X, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-    k_wgrad<X, G><<<grid, TM, smem, st>>>(a);                                                       \
-  } while (0)
+#define WG(X, G) k_wgrad<X, G><<<grid, TM, smem, st>>>(a)
   if (vx && vg) WG(true, true);
   else if (vx) WG(true, false);
   else if (vg) WG(false, true);
   else WG(false, false);
 #undef WG
   CCUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
+// the largest tile (N = 128) needs 64 KiB of dynamic shared memory
+int set_attrs() {
+  const int big = (int)conv_smem(128);
+  CCUDA(cudaFuncSetAttribute(k_conv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_conv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_wgrad<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_wgrad<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_wgrad<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_wgrad<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   return PQG_OK;
 }
 
@@ -662,7 +665,7 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
   }
   cudaMemcpy(net->norm, nm.data(), 4 * nm.size(), cudaMemcpyHostToDevice);
   cudaMemset(net->err, 0, 4);
-  if (cudaDeviceSynchronize() != cudaSuccess) return fail("initialisation");
+  if (set_attrs() != PQG_OK || cudaDeviceSynchronize() != cudaSuccess) return fail("initialisation");
   *out = net;
   return PQG_OK;
 }
@@ -685,6 +688,16 @@ PQG_API int pqg_cnn_destroy(pqg_cnn* net) {
   cudaFree(net->loss);
   cudaFree(net->err);
   delete net;
+  return PQG_OK;
+}
+
+PQG_API int pqg_cnn_shape(pqg_cnn* net, int* cin, int* cout, int* ny, int* nx, int* max_batch) {
+  if (!net) return cfail(PQG_ERR_INVALID, "NULL argument");
+  if (cin) *cin = net->L.front().cin;
+  if (cout) *cout = net->L.back().cout;
+  if (ny) *ny = net->H;
+  if (nx) *nx = net->W;
+  if (max_batch) *max_batch = net->maxB;
   return PQG_OK;
 }
 

@@ -106,7 +106,8 @@ __device__ __forceinline__ size_t sidx(int b, int z, int l, int k, int nz, int n
 // ---------------------------------------------------------------------------
 template <class V, int LOGM>
 __global__ void e_row_adv(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, const typename Sc<V>::T* qphys,
-                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb) {
+                          const V* __restrict__ twx, typename Sc<V>::T scale, int rb,
+                          typename Sc<V>::T* qout) {
   typedef typename Sc<V>::T S;
   constexpr int M = 1 << LOGM;
   extern __shared__ __align__(16) unsigned char esm[];
@@ -143,6 +144,10 @@ __global__ void e_row_adv(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, cons
     V u = cscale(bU[t], scale), v = cscale(bV[t], scale);
     V q = bQ[t];
     if (!qphys) q = cscale(q, scale);
+    if (qout) {
+      const int rr = t / M, m = t - rr * M;
+      *reinterpret_cast<V*>(qout + (size_t)(r0 + rr) * nx + 2 * m) = q;
+    }
     bU[t] = mk(smul(sadd(u.x, ub), q.x), smul(sadd(u.y, ub), q.y));
     bV[t] = mk(smul(v.x, q.x), smul(v.y, q.y));
   }
@@ -158,12 +163,15 @@ __global__ void e_row_adv(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, cons
 // ---------------------------------------------------------------------------
 // fused column kernel: grid (nz, ceil(nk / C), B), cluster (nz, 1, 1); each
 // CTA handles C consecutive columns of one layer of one member.  Shared:
-// [tw (ny)] [U: C][V: C][QN: C][QO: C] sequences of ny.
+// [tw (ny)] [U: C][V: C][X: C][QO: C] sequences of ny, where X first holds
+// the mixed subgrid forcing F (when `forcing`), transformed with U and V and
+// added to the tendency after the drag (the q_parameterization order,
+// pyqg/model.py:406-436), then the new qh.
 // ---------------------------------------------------------------------------
 template <class V, int LOGN>
 __global__ void e_col_fused(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, V* qh, const V* dqp,
                             V* dqpp, const V* __restrict__ twy, typename Sc<V>::T c1,
-                            typename Sc<V>::T c2, typename Sc<V>::T c3, int C) {
+                            typename Sc<V>::T c2, typename Sc<V>::T c3, int C, int forcing) {
   typedef typename Sc<V>::T S;
   constexpr int N = 1 << LOGN;
   extern __shared__ __align__(16) unsigned char esm[];
@@ -173,12 +181,13 @@ __global__ void e_col_fused(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, V*
   V* tw = reinterpret_cast<V*>(esm);
   V* bU = tw + ny;
   V* bV = bU + C * ny;
-  V* bQN = bV + C * ny;
+  V* bQN = bV + C * ny;   // X
   V* bQO = bQN + C * ny;
   const size_t plane = (size_t)ny * nk;
   V* mU = scratch + b * g.mstride + (size_t)z * plane;
   V* mV = mU + (size_t)nz * plane;
   V* mQ = mV + (size_t)nz * plane;
+  const V* mF = mQ + (size_t)nz * plane;
   for (int i = threadIdx.x; i < ny; i += blockDim.x) tw[i] = twy[i];
   for (int t = threadIdx.x; t < C * ny; t += blockDim.x) {
     const int cc = t / ny, l = t - cc * ny, k = k0 + cc;
@@ -186,10 +195,11 @@ __global__ void e_col_fused(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, V*
     const size_t mo = (size_t)k * ny + l;
     bU[t] = ok ? mU[mo] : mk((S)0, (S)0);
     bV[t] = ok ? mV[mo] : mk((S)0, (S)0);
+    if (forcing) bQN[t] = ok ? mF[mo] : mk((S)0, (S)0);
     bQO[t] = ok ? qh[sidx(b, z, l, k, nz, ny, nk)] : mk((S)0, (S)0);
   }
   __syncthreads();
-  Pow2Fft<N, 1, false, V>::run(bU, ny, 2 * C, tw, 1);
+  Pow2Fft<N, 1, false, V>::run(bU, ny, (forcing ? 3 : 2) * C, tw, 1);
   cluster.sync();
   const S rek = c.rek[b];
   const bool drag = (rek != (S)0) && (z == nz - 1);
@@ -206,6 +216,10 @@ __global__ void e_col_fused(EGeo g, EConsts<typename Sc<V>::T> c, V* scratch, V*
     const S kk = c.kk[k], kQy = c.kQy[((size_t)b * nz + z) * nk + k];
     V d = g_tendency(kk, c.ll[l], kQy, bU[t], bV[t], p);
     if (drag) d = g_friction(d, smul(rek, c.k2l2[ck]), p);
+    if (forcing) {
+      const V f = bQN[t];
+      d = mk(sadd(d.x, f.x), sadd(d.y, f.y));
+    }
     const V pv = dqp[o], ppv = dqpp[o];
     const V qn = g_ab(c.filtr[ck], bQO[t], d, pv, ppv, c1, c2, c3);
     qh[o] = qn;
@@ -303,7 +317,8 @@ __global__ void e_row_c2r(EGeo g, const V* scratch, int field, typename Sc<V>::T
 
 // physical (B, nz, ny, nx) -> mixed plane 0 of every member
 template <class V, int LOGM>
-__global__ void e_row_r2c(EGeo g, V* scratch, const typename Sc<V>::T* phys, const V* __restrict__ twx, int rb) {
+__global__ void e_row_r2c(EGeo g, V* scratch, const typename Sc<V>::T* phys, const V* __restrict__ twx, int rb,
+                          int field) {
   constexpr int M = 1 << LOGM;
   extern __shared__ __align__(16) unsigned char esm[];
   V* tw = reinterpret_cast<V*>(esm);
@@ -312,7 +327,7 @@ __global__ void e_row_r2c(EGeo g, V* scratch, const typename Sc<V>::T* phys, con
   const int r0 = blockIdx.x * rb;
   const int b = r0 / rows_m, rm = r0 - b * rows_m, z = rm / ny, y0 = rm - z * ny;
   const size_t plane = (size_t)ny * g.nk;
-  V* base = scratch + b * g.mstride + (size_t)z * plane + y0;
+  V* base = scratch + b * g.mstride + ((size_t)field * g.nz + z) * plane + y0;
   for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
   for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
     const int rr = t / M, m = t - rr * M;
@@ -428,6 +443,10 @@ struct pqg_ens {
   long long tc = 0;
   double t = 0.0, dt = 0.0;
   int T_row = 128, rb = 1, T_col = 128, C = 1;
+  int nfield = 3;               // mixed planes per member: U, V, Q (+ forcing F)
+  pqg_cnn* net = nullptr;       // closure: forcing = net(q) every step
+  void* qcur = nullptr;         // physical q of the current step (closure input)
+  void* dqf = nullptr;          // closure output, physical
   std::vector<double> h_kk, h_Qy;  // for kQy
   bool have_consts = false, have_members = false;
 };
@@ -482,11 +501,11 @@ int lg2(int n) { int l = 0; while ((1 << l) < n) l++; return l; }
 template <class V>
 struct EK {
   typedef typename Sc<V>::T S;
-  typedef void (*RowAdv)(EGeo, EConsts<S>, V*, const S*, const V*, S, int);
-  typedef void (*ColFused)(EGeo, EConsts<S>, V*, V*, const V*, V*, const V*, S, S, S, int);
+  typedef void (*RowAdv)(EGeo, EConsts<S>, V*, const S*, const V*, S, int, S*);
+  typedef void (*ColFused)(EGeo, EConsts<S>, V*, V*, const V*, V*, const V*, S, S, S, int, int);
   typedef void (*ColInv)(EGeo, EConsts<S>, V*, const V*, const V*, int);
   typedef void (*RowC2r)(EGeo, const V*, int, S*, const V*, S, int);
-  typedef void (*RowR2c)(EGeo, V*, const S*, const V*, int);
+  typedef void (*RowR2c)(EGeo, V*, const S*, const V*, int, int);
   typedef void (*ColFwd)(EGeo, const V*, V*, const V*, int);
   static RowAdv row_adv(int M) {
     switch (lg2(M)) {
@@ -549,7 +568,7 @@ EConsts<typename Sc<V>::T> econsts(const pqg_ens* e) {
 EGeo egeo(const pqg_ens* e) {
   EGeo g;
   g.B = e->B; g.nz = e->nz; g.ny = e->ny; g.nx = e->nx; g.nk = e->nk; g.M = e->M;
-  g.mstride = (size_t)3 * e->nz * e->ny * e->nk;
+  g.mstride = (size_t)e->nfield * e->nz * e->ny * e->nk;
   return g;
 }
 size_t vsz(const pqg_ens* e) { return 2 * e->esz; }
@@ -561,7 +580,7 @@ int launch_row_adv(pqg_ens* e, bool first, cudaStream_t st) {
   const size_t smem = vsz(e) * ((size_t)e->nx + 3 * (size_t)e->rb * e->M);
   EK<V>::row_adv(e->M)<<<(nrows + e->rb - 1) / e->rb, e->T_row, smem, st>>>(
       egeo(e), econsts<V>(e), (V*)e->scratch, first ? (const S*)e->q : nullptr, (const V*)e->twx,
-      (S)(1.0 / ((double)e->nx * e->ny)), e->rb);
+      (S)(1.0 / ((double)e->nx * e->ny)), e->rb, e->net ? (S*)e->qcur : nullptr);
   ECUDA(cudaGetLastError());
   return PQG_OK;
 }
@@ -587,7 +606,7 @@ int launch_col_fused(pqg_ens* e, cudaStream_t st) {
   cfg.numAttrs = 1;
   ECUDA(cudaLaunchKernelEx(&cfg, EK<V>::col_fused(e->ny), egeo(e), econsts<V>(e), (V*)e->scratch, (V*)e->qh,
                            (const V*)e->dq[e->role_p], (V*)e->dq[e->role_pp], (const V*)e->twy, (S)c1, (S)c2,
-                           (S)c3, e->C));
+                           (S)c3, e->C, e->net ? 1 : 0));
   // rotation: newest tendency in the old pp buffer
   std::swap(e->role_p, e->role_pp);
   e->ablevel = e->ablevel >= 2 ? 2 : e->ablevel + 1;
@@ -616,11 +635,27 @@ int launch_epilogue(pqg_ens* e, cudaStream_t st) {
   return PQG_OK;
 }
 
+// closure: forcing = net(q) (physical), then its row transforms into mixed
+// plane 3 (the column transforms run inside the fused column kernel)
+template <class V>
+int launch_closure(pqg_ens* e, cudaStream_t st) {
+  typedef typename Sc<V>::T S;
+  const int f64 = e->prec == 8 ? 1 : 0;
+  if (pqg_cnn_forward(e->net, e->qcur, f64, e->dqf, f64, e->B, st) != PQG_OK)
+    return efail(PQG_ERR_CUDA, std::string("closure network: ") + pqg_cnn_last_error());
+  const int nrows = e->B * e->nz * e->ny;
+  EK<V>::row_r2c(e->M)<<<(nrows + e->rb - 1) / e->rb, e->T_row, vsz(e) * ((size_t)e->nx + (size_t)e->rb * e->M),
+                         st>>>(egeo(e), (V*)e->scratch, (const S*)e->dqf, (const V*)e->twx, e->rb, 3);
+  ECUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
 template <class V>
 int step_impl(pqg_ens* e, int nsteps, cudaStream_t st) {
   int rc = launch_prologue<V>(e, st);
   for (int i = 0; i < nsteps && !rc; i++) {
     rc = launch_row_adv<V>(e, i == 0, st);
+    if (!rc && e->net) rc = launch_closure<V>(e, st);
     if (!rc) rc = launch_col_fused<V>(e, st);
   }
   if (!rc) rc = launch_epilogue<V>(e, st);
@@ -637,7 +672,7 @@ int set_q_impl(pqg_ens* e, cudaStream_t st) {
   ECUDA(cudaGetLastError());
   const int nrows = e->B * e->nz * e->ny;
   EK<V>::row_r2c(e->M)<<<(nrows + e->rb - 1) / e->rb, e->T_row, vsz(e) * ((size_t)e->nx + (size_t)e->rb * e->M), st>>>(
-      egeo(e), (V*)e->scratch, (const S*)e->q, (const V*)e->twx, e->rb);
+      egeo(e), (V*)e->scratch, (const S*)e->q, (const V*)e->twx, e->rb, 0);
   ECUDA(cudaGetLastError());
   EK<V>::col_fwd(e->ny)<<<dim3(e->nz, (e->nk + e->C - 1) / e->C, e->B), e->T_col,
                            vsz(e) * (size_t)e->ny * (1 + e->C), st>>>(
@@ -711,7 +746,7 @@ PQG_API int pqg_ens_create(pqg_ens** out, int nmembers, int nz, int ny, int nx, 
 PQG_API int pqg_ens_destroy(pqg_ens* e) {
   if (!e) return PQG_OK;
   void* ps[] = {e->twx, e->twy, e->a, e->kk, e->ll, e->k2l2, e->filtr, e->kQy, e->Ubg, e->rek, e->q,
-                e->qh, e->dq[0], e->dq[1], e->dq[2], e->scratch, e->d_red};
+                e->qh, e->dq[0], e->dq[1], e->dq[2], e->scratch, e->d_red, e->qcur, e->dqf};
   for (void* p : ps) cudaFree(p);
   delete e;
   return PQG_OK;
@@ -844,6 +879,37 @@ PQG_API int pqg_ens_energy(pqg_ens* e, double* ke, double* ens, void* stream) {
   ECUDA(cudaMemcpyAsync(ke, dk, sizeof(double) * e->B * e->nz, cudaMemcpyDeviceToHost, st));
   ECUDA(cudaMemcpyAsync(ens, de, sizeof(double) * e->B * e->nz, cudaMemcpyDeviceToHost, st));
   ECUDA(cudaStreamSynchronize(st));
+  return PQG_OK;
+}
+
+PQG_API int pqg_ens_set_closure(pqg_ens* e, pqg_cnn* net) {
+  if (!e) return efail(PQG_ERR_INVALID, "NULL argument");
+  if (cudaDeviceSynchronize() != cudaSuccess) return efail(PQG_ERR_CUDA, "device error before pqg_ens_set_closure");
+  if (!net) {
+    e->net = nullptr;
+    return PQG_OK;
+  }
+  int cin = 0, cout = 0, ny = 0, nx = 0, maxb = 0;
+  if (pqg_cnn_shape(net, &cin, &cout, &ny, &nx, &maxb) != PQG_OK) return efail(PQG_ERR_INVALID, "bad network");
+  if (cin != e->nz || cout != e->nz || ny != e->ny || nx != e->nx)
+    return efail(PQG_ERR_INVALID, "network channels / image size must match the members' (nz, ny, nx)");
+  if (maxb < e->B) return efail(PQG_ERR_INVALID, "network batch capacity below the member count");
+  const size_t S = (size_t)e->B * e->nz * e->ny * e->nk, P = (size_t)e->B * e->nz * e->ny * e->nx;
+  const size_t V = 2 * e->esz;
+  if (e->nfield < 4) {
+    void* ns = nullptr;
+    if (cudaMalloc(&ns, std::max(V * 4 * S, sizeof(double) * P)) != cudaSuccess)
+      return efail(PQG_ERR_NOMEM, "cudaMalloc failed in pqg_ens_set_closure");
+    cudaMemset(ns, 0, std::max(V * 4 * S, sizeof(double) * P));
+    cudaFree(e->scratch);
+    e->scratch = ns;
+    e->nfield = 4;
+  }
+  if (!e->qcur && cudaMalloc(&e->qcur, e->esz * P) != cudaSuccess)
+    return efail(PQG_ERR_NOMEM, "cudaMalloc failed in pqg_ens_set_closure");
+  if (!e->dqf && cudaMalloc(&e->dqf, e->esz * P) != cudaSuccess)
+    return efail(PQG_ERR_NOMEM, "cudaMalloc failed in pqg_ens_set_closure");
+  e->net = net;
   return PQG_OK;
 }
 

@@ -423,6 +423,62 @@ __global__ void k_add_uv(Geo g, Consts c, const double2* __restrict__ duh,
   }
 }
 
+// products u f and v f of physical planes (pyqg/model.py:546-547)
+__global__ void k_products(size_t n, const double* __restrict__ f, const double* __restrict__ u,
+                           const double* __restrict__ v, double* __restrict__ uf, double* __restrict__ vf) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double x = f[i];
+    uf[i] = __dmul_rn(u[i], x);
+    vf[i] = __dmul_rn(v[i], x);
+  }
+}
+
+// spectral advective tendency ik A + il B of A = fft(u f), B = fft(v f)
+// (pyqg/model.py:553); (0 + ik)(a + ib) = -k b + i k a exactly
+__global__ void k_adv_combine(int nplanes, int ny, int nk, const double* __restrict__ kk,
+                              const double* __restrict__ ll, const double2* __restrict__ A,
+                              const double2* __restrict__ B, double2* __restrict__ out) {
+  const size_t n = (size_t)nplanes * ny * nk;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % nk);
+    const int l = (int)((i / nk) % ny);
+    const double2 a = A[i], b = B[i];
+    const double kx = kk[k], ly = ll[l];
+    out[i] = make_double2(__dadd_rn(-__dmul_rn(kx, a.y), -__dmul_rn(ly, b.y)),
+                          __dadd_rn(__dmul_rn(kx, a.x), __dmul_rn(ly, b.x)));
+  }
+}
+
+// sharp spectral truncation of (nplanes, nyf, nkf) to (nplanes, nyc, nkc):
+// wavenumbers |k| < nxc / 2 and |l| < nyc / 2 are kept (times `scale`, the
+// ratio of the grids' point counts, so that physical amplitudes are kept);
+// the coarse grid's Nyquist row and column are zero.
+__global__ void k_truncate(int nplanes, int nyf, int nkf, const double2* __restrict__ in, int nyc, int nkc,
+                           double2* __restrict__ out, double scale) {
+  const size_t n = (size_t)nplanes * nyc * nkc;
+  const int nyc2 = nyc / 2;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % nkc);
+    const int l = (int)((i / nkc) % nyc);
+    const size_t pl = i / ((size_t)nkc * nyc);
+    double2 v = make_double2(0.0, 0.0);
+    if (k < nkc - 1 && l != nyc2) {
+      const int lf = l < nyc2 ? l : nyf - (nyc - l);
+      const double2 x = in[(pl * nyf + lf) * nkf + k];
+      v = make_double2(__dmul_rn(x.x, scale), __dmul_rn(x.y, scale));
+    }
+    out[i] = v;
+  }
+}
+
+__global__ void k_csub(size_t n, const double2* __restrict__ a, const double2* __restrict__ b,
+                       double2* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double2 x = a[i], y = b[i];
+    out[i] = make_double2(__dsub_rn(x.x, y.x), __dsub_rn(x.y, y.y));
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Fused column kernel of one time step.  Grid (nz, nk), cluster (nz, 1, 1):
 // the CTA of layer z = cluster rank z handles column k of that layer.
@@ -839,6 +895,8 @@ struct pqg_plan {
   int log2_nxny = 0;
   double2* scratch = nullptr;  // mixed planes
   int scratch_planes = 0;
+  double2* work = nullptr;     // planes for advection / coarse-graining temporaries
+  int work_planes = 0;
   int T_row = 128, rb = 1, T_col = 256;
   int T_row_batch = 128, rb_batch = 1;
   cudaStream_t cap_stream = nullptr;
@@ -958,6 +1016,18 @@ static int ensure_scratch(pqg_plan* p, int planes) {
   if (cudaMalloc(&p->scratch, bytes) != cudaSuccess)
     return fail(PQG_ERR_NOMEM, "cudaMalloc scratch failed");
   p->scratch_planes = planes;
+  return PQG_OK;
+}
+
+// work planes are grown on demand (between calls; never inside a capture)
+static int ensure_work(pqg_plan* p, int planes) {
+  if (planes <= p->work_planes) return PQG_OK;
+  cudaFree(p->work);
+  p->work = nullptr;
+  p->work_planes = 0;
+  const size_t bytes = sizeof(double2) * (size_t)planes * p->ny * p->nk;
+  if (cudaMalloc(&p->work, bytes) != cudaSuccess) return fail(PQG_ERR_NOMEM, "cudaMalloc work planes failed");
+  p->work_planes = planes;
   return PQG_OK;
 }
 
@@ -1334,6 +1404,7 @@ PQG_API int pqg_plan_destroy(pqg_plan* p) {
   cudaFree(p->twx); cudaFree(p->twy); cudaFree(p->a); cudaFree(p->kk);
   cudaFree(p->ll); cudaFree(p->k2l2); cudaFree(p->kQy); cudaFree(p->Ubg);
   cudaFree(p->filtr); cudaFree(p->scratch); cudaFree(p->twx_q); cudaFree(p->twy_q);
+  cudaFree(p->work);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   delete p;
   return PQG_OK;
@@ -1800,6 +1871,97 @@ PQG_API int pqg_rfft2_noalloc(const double* x, double* xh, int nplanes, int ny, 
   p.twx = p.twy = nullptr;  // not owned: keep the plan destructor-free path
   p.scratch = nullptr;
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// advection of arbitrary fields and spectral coarse-graining (FP64 transforms)
+// ---------------------------------------------------------------------------
+static unsigned grid_of(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 32); }
+
+// out = ik fft(u f) + il fft(v f); tmp holds 4 * nplanes planes
+static int advect_into(pqg_plan* p, const double* f, const double* u, const double* v, int nplanes,
+                       double2* out, double2* tmp, cudaStream_t st) {
+  const size_t pc = (size_t)p->ny * p->nk, pr = (size_t)p->ny * p->nx;
+  double* uf = reinterpret_cast<double*>(tmp);
+  double* vf = reinterpret_cast<double*>(tmp + nplanes * pc);
+  double2* A = tmp + 2 * nplanes * pc;
+  double2* B = tmp + 3 * nplanes * pc;
+  // the physical products are packed plane after plane (stride ny * nx)
+  const size_t n = (size_t)nplanes * pr;
+  k_products<<<grid_of(n), 256, 0, st>>>(n, f, u, v, uf, vf);
+  CHECK_LAUNCH();
+  int rc = pqg_rfft2(p, uf, reinterpret_cast<double*>(A), nplanes, st);
+  if (!rc) rc = pqg_rfft2(p, vf, reinterpret_cast<double*>(B), nplanes, st);
+  if (rc) return rc;
+  k_adv_combine<<<grid_of(nplanes * pc), 256, 0, st>>>(nplanes, p->ny, p->nk, p->kk, p->ll, A, B, out);
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
+// u, v (physical) of spectral PV qh with FP64 transforms
+static int velocities(pqg_plan* p, const double2* qh, double* u, double* v, cudaStream_t st) {
+  const size_t pc = (size_t)p->ny * p->nk;
+  double2* mU = p->scratch;
+  double2* mV = p->scratch + p->nz * pc;
+  dim3 grid(p->nz, p->nk);
+  col_invert_kernel(0, p->ny)<<<grid, p->T_col, col_smem(p, 2), st>>>(geo(p), consts(p), qh, nullptr, nullptr,
+                                                                      nullptr, mU, mV, p->twy_q);
+  CHECK_LAUNCH();
+  int rc = launch_row_c2r(p, mU, u, p->nz, st, 0);
+  if (!rc) rc = launch_row_c2r(p, mV, v, p->nz, st, 0);
+  return rc;
+}
+
+PQG_API int pqg_advect(pqg_plan* p, const double* f, const double* u, const double* v, int nplanes,
+                       double* out_h, void* stream) {
+  if (!p || !f || !u || !v || !out_h || nplanes < 1) return fail(PQG_ERR_INVALID, "bad argument to pqg_advect");
+  if (!p->have_kk || !p->have_ll) return fail(PQG_ERR_STATE, "wavenumbers not set");
+  int rc = ensure_work(p, 4 * nplanes);
+  if (rc) return rc;
+  return advect_into(p, f, u, v, nplanes, dc(out_h), p->work, (cudaStream_t)stream);
+}
+
+PQG_API int pqg_coarse_forcing(pqg_plan* pf, pqg_plan* pc, const double* qh_f, double* q_c, double* S,
+                               void* stream) {
+  if (!pf || !pc || !qh_f || !q_c || !S) return fail(PQG_ERR_INVALID, "NULL argument to pqg_coarse_forcing");
+  if (pf->nz != pc->nz) return fail(PQG_ERR_INVALID, "layer counts differ");
+  if (pc->nx > pf->nx || pc->ny > pf->ny || (pc->nx & 1) || (pc->ny & 1))
+    return fail(PQG_ERR_INVALID, "coarse grid must be even and not finer than the fine grid");
+  if (!pf->have_kk || !pf->have_ll || !pc->have_kk || !pc->have_ll) return fail(PQG_ERR_STATE, "wavenumbers not set");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nz = pf->nz;
+  int rc = ensure_work(pf, 8 * nz);
+  if (!rc) rc = ensure_work(pc, 9 * nz);
+  if (rc) return rc;
+  const size_t sf = (size_t)nz * pf->ny * pf->nk, sc = (size_t)nz * pc->ny * pc->nk;
+  // fine: u, v, q, J = ik fft(u q) + il fft(v q)
+  double* uf = reinterpret_cast<double*>(pf->work);
+  double* vf = reinterpret_cast<double*>(pf->work + sf);
+  double* qf = reinterpret_cast<double*>(pf->work + 2 * sf);
+  double2* Jf = pf->work + 3 * sf;
+  rc = velocities(pf, dc(qh_f), uf, vf, st);
+  if (!rc) rc = pqg_irfft2(pf, qh_f, qf, nz, st);
+  if (!rc) rc = advect_into(pf, qf, uf, vf, nz, Jf, pf->work + 4 * sf, st);
+  if (rc) return rc;
+  // truncate J and qh
+  const double scale = ((double)pc->nx * pc->ny) / ((double)pf->nx * pf->ny);
+  double2* Jbar = pc->work;
+  double2* qbar = pc->work + sc;
+  k_truncate<<<grid_of(sc), 256, 0, st>>>(nz, pf->ny, pf->nk, Jf, pc->ny, pc->nk, Jbar, scale);
+  k_truncate<<<grid_of(sc), 256, 0, st>>>(nz, pf->ny, pf->nk, dc(qh_f), pc->ny, pc->nk, qbar, scale);
+  CHECK_LAUNCH();
+  // coarse: q, u, v of the truncated PV and their advection
+  double* ubar = reinterpret_cast<double*>(pc->work + 2 * sc);
+  double* vbar = reinterpret_cast<double*>(pc->work + 3 * sc);
+  double2* Jc = pc->work + 4 * sc;
+  rc = pqg_irfft2(pc, reinterpret_cast<const double*>(qbar), q_c, nz, st);
+  if (!rc) rc = velocities(pc, qbar, ubar, vbar, st);
+  if (!rc) rc = advect_into(pc, q_c, ubar, vbar, nz, Jc, pc->work + 5 * sc, st);
+  if (rc) return rc;
+  // S = filtered(J(psi, q)) - J(filtered psi, filtered q)
+  k_csub<<<grid_of(sc), 256, 0, st>>>(sc, Jbar, Jc, qbar);   // qbar no longer needed
+  CHECK_LAUNCH();
+  return pqg_irfft2(pc, reinterpret_cast<const double*>(qbar), S, nz, st);
 }
 
 }  // extern "C"

@@ -118,6 +118,12 @@ class EnsembleGroup:
         self._check(self._L.pqg_ens_energy(self._h, ke.ctypes.data, en.ctypes.data, self._sp()))
         return ke, en
 
+    def set_closure(self, net):
+        """Attach a :class:`~pyqg_gb300.closure.ConvNet` (or None): every step
+        adds its PV forcing, as a q_parameterization would."""
+        self._net = net
+        self._check(self._L.pqg_ens_set_closure(self._h, None if net is None else net._h))
+
     def state(self):
         q, qh = ctypes.c_void_p(), ctypes.c_void_p()
         tc, t = ctypes.c_longlong(), ctypes.c_double()
@@ -192,6 +198,16 @@ class Ensemble:
         rc = L.pqg_ens_step_many(arr, len(self.groups), int(nsteps), self.groups[0]._sp())
         self.groups[0]._check(rc)
         self.tc += nsteps
+
+    def set_closure(self, net):
+        """Attach a learned closure to every group whose members match the
+        network's channels and image size; returns the number of groups."""
+        n = 0
+        for grp in self.groups:
+            if net is None or (grp.nz == net.channels[0] == net.channels[-1] and grp.nx == net.nx):
+                grp.set_closure(net)
+                n += 1
+        return n
 
     def energy(self):
         """FP64 (ke, enstrophy) per member and layer, in member order."""

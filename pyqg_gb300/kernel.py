@@ -242,6 +242,15 @@ class PseudoSpectralKernel:
                                      x.shape[0], self._sp()))
         return out
 
+    def _device_advect(self, f, u, v):
+        """ik fft(u f) + il fft(v f) of device real fields (n, ny, nx)."""
+        f, u, v = (t.to(self._device, torch.float64).contiguous() for t in (f, u, v))
+        out = torch.empty((f.shape[0], self.nl, self.nk), dtype=torch.complex128,
+                          device=self._device)
+        _lib.check(self._L.pqg_advect(self._plan, f.data_ptr(), u.data_ptr(), v.data_ptr(),
+                                      f.shape[0], out.data_ptr(), self._sp()))
+        return out
+
     def _device_irfft2(self, xh):
         xh = xh.contiguous()
         out = torch.empty((xh.shape[0], self.ny, self.nx), dtype=torch.float64,

@@ -260,16 +260,26 @@ class Model(PseudoSpectralKernel):
     # ------------------------------------------------------------------
     def _advect(self, q, u=None, v=None):
         """Spectral advective tendency ik (uq)^ + il (vq)^ of real q
-        (``pyqg/model.py:539-558``); 2-D inputs give a 2-D result."""
-        u = self.u if u is None else u
-        v = self.v if v is None else v
-        uq, vq = u * q, v * q
-        flat = uq.ndim == 2
-        if flat:
-            uq, vq = uq[np.newaxis], vq[np.newaxis]
-        tend = self.ik * self.fft(np.ascontiguousarray(uq)) + \
-            self.il * self.fft(np.ascontiguousarray(vq))
-        return tend[0] if flat else tend
+        (``pyqg/model.py:539-558``); 2-D inputs give a 2-D result.  The
+        products, transforms and derivatives run on the GPU; numpy inputs
+        give a numpy result, CUDA tensors a CUDA tensor."""
+        import torch
+        on_device = any(isinstance(x, torch.Tensor) for x in (q, u, v))
+        if u is None:
+            u = self.device_field("u") if on_device else self.u
+        if v is None:
+            v = self.device_field("v") if on_device else self.v
+        arrs = [x if isinstance(x, torch.Tensor) else torch.from_numpy(np.asarray(x, dtype=np.float64))
+                for x in (q, u, v)]
+        shape = torch.broadcast_shapes(*(a.shape for a in arrs))
+        flat = len(shape) == 2
+        with torch.cuda.stream(self._stream):
+            arrs = [a.to(self._device, torch.float64).broadcast_to(shape).reshape(-1, self.ny, self.nx)
+                    for a in arrs]
+            tend = self._device_advect(*arrs)
+            if flat:
+                tend = tend[0]
+            return tend if on_device else tend.cpu().numpy()
 
     def _print_status(self):
         """Log KE and CFL every `twrite` steps; fail if CFL >= 1."""

@@ -155,3 +155,48 @@ def test_cnn_parameterization_in_model(quiet):
         m._step_forward()
     assert np.all(np.isfinite(m.q))
     assert m.tc == 5
+
+
+def test_ensemble_closure_matches_single_models(quiet):
+    """FP64 ensemble members with the closure attached step like single
+    FP64-engine models with the same net as q_parameterization."""
+    import pyqg_gb300 as P
+    from pyqg_gb300.closure import ConvNet, CNNParameterization
+    from pyqg_gb300.coarsen import PHYSICS
+    net = ConvNet(max_batch=2, seed=11)
+    stats = ([0.0, 0.0], [3e-7, 3e-8], [0.0, 0.0], [3e-13, 3e-14])
+    param = CNNParameterization(net, stats)
+    rng = np.random.default_rng(9)
+    qs = [1e-7 * rng.standard_normal((2, 64, 64)) for _ in range(2)]
+    ens = P.Ensemble([("qg", dict(nx=64, dt=7200.0, **PHYSICS))] * 2, precision="fp64")
+    ens.set_q(qs)
+    assert ens.set_closure(net) == 1
+    ens.step(6)
+    for i in range(2):
+        m = P.QGModel(nx=64, dt=7200.0, q_parameterization=param, **PHYSICS, **quiet)
+        m.engine = "fp64"
+        m.q = qs[i]
+        for _ in range(6):
+            m._step_forward()
+        assert rel_l2(ens.q(i), m.q) < 1e-13
+    # the closure changes the trajectory
+    ens2 = P.Ensemble([("qg", dict(nx=64, dt=7200.0, **PHYSICS))] * 2, precision="fp64")
+    ens2.set_q(qs)
+    ens2.step(6)
+    assert rel_l2(ens2.q(0), ens.q(0)) > 1e-8
+
+
+def test_ensemble_closure_fp32_runs():
+    import torch
+    import pyqg_gb300 as P
+    from pyqg_gb300.closure import ConvNet, CNNParameterization
+    from pyqg_gb300.coarsen import PHYSICS
+    net = ConvNet(max_batch=8, seed=12)
+    CNNParameterization(net, ([0.0, 0.0], [3e-7, 3e-8], [0.0, 0.0], [3e-13, 3e-14]))
+    rng = np.random.default_rng(10)
+    ens = P.Ensemble([("qg", dict(nx=64, dt=7200.0, **PHYSICS))] * 8, precision="fp32")
+    ens.set_q([1e-7 * rng.standard_normal((2, 64, 64)) for _ in range(8)])
+    ens.set_closure(net)
+    ens.step(20)
+    torch.cuda.synchronize()
+    assert all(np.all(np.isfinite(ens.q(i))) for i in range(8))
