@@ -8,25 +8,36 @@
 // Every convolution is an implicit GEMM over K = (tap, channel):
 //   forward  out[p][co] = sum_{tap,ci} in[p + off(tap)][ci] w[co][tap][ci]
 //   dgrad    din[p][ci] = sum_{tap,co} g[p + off(tap)][co] w[co][24-tap][ci]
-//            (the forward kernel with flipped, channel-transposed weights)
+//            (a forward convolution with flipped, channel-transposed weights)
 //   wgrad    dw[co][tap][ci] = sum_p x[p + off(tap)][ci] g[p][co]
 // with off(tap) = (tap / 5 - 2, tap % 5 - 2) taken periodically.
-// Activations are NHWC BF16 (channels contiguous); master weights are FP32
-// w[co][tap][ci]; packed BF16 copies hold each K chunk of 64 as one
-// contiguous block in the tensor core's K-major core-matrix layout.
 //
-// A CTA of 128 threads owns a tile of 128 rows (pixels for forward/dgrad,
-// (tap, channel) pairs for wgrad) and all N columns.  K advances in chunks of
-// 64 through two shared-memory stages: the threads gather a chunk, one
-// thread issues four 128xNx16 MMAs and commits them to the stage's mbarrier,
-// and the stage is refilled once that barrier completes.  The epilogue reads
-// the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31).
+// Activations and gradients are BF16 NHWC images stored with a periodic
+// halo of 2 pixels on each side ((ny + 4) x (nx + 4) pixels per image, the
+// halo a copy of the opposite edge), written by every producer, so that no
+// consumer wraps indices.  Master weights are FP32 w[co][tap][ci].
+//
+// Two convolution kernels:
+//  * k_conv_halo (input channels a multiple of 16): a CTA computes a tile of
+//    16 rows x 8 SX columns.  TMA loads the input tile with its halo once into
+//    shared memory as one slab per 8 channels (pixel-major, 16 bytes per
+//    pixel); the A operand of tap (dy, dx) is then a shifted descriptor over
+//    the same slabs (core matrix = 8 consecutive pixels of a row, next
+//    8-pixel group = next image row).  The per-tap weight blocks stream
+//    through a 3-stage bulk-copy pipeline; one thread issues the MMAs.
+//  * k_conv_gather (few input channels, e.g. the 2-channel input layer):
+//    threads gather a K-chunk of 64 (tap, channel) pairs per pixel.
+// The weight gradient gathers (tap, channel) x pixel tiles (k_wgrad) and
+// adds its partial sums atomically.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -41,10 +52,14 @@ namespace tc = pqg::tc;
 
 namespace {
 
-constexpr int KC = 64;     // K elements per chunk
+constexpr int KC = 64;     // K elements per chunk (gather kernels)
 constexpr int TM = 128;    // tile rows
 constexpr int NTAP = 25;   // 5 x 5 taps
-constexpr int CHUNK_A = TM * KC * 2;   // bytes of one A stage
+constexpr int PAD = 2;     // halo width
+constexpr int CHUNK_A = TM * KC * 2;   // bytes of one A stage (gather kernels)
+constexpr int TY = 16;     // output rows of a halo-kernel tile
+constexpr int TYH = TY + 2 * PAD;
+constexpr int NST = 3;     // weight stages of the halo kernel
 
 thread_local std::string c_last_error;
 
@@ -61,32 +76,219 @@ int cfail(int code, const std::string& msg) {
 
 __host__ __device__ inline int pad16(int n) { return (n + 15) & ~15; }
 
-__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+struct Img {            // padded NHWC image geometry
+  int H, W, Hp, Wp;
+  __device__ __forceinline__ size_t pix(int b, int yp, int xp) const {
+    return ((size_t)b * Hp + yp) * Wp + xp;
+  }
+};
 
-// ---------------------------------------------------------------------------
-// forward / dgrad convolution
-// ---------------------------------------------------------------------------
-struct ConvArgs {
-  const bf16* in;        // NHWC, cin channels
-  int cin;
-  const bf16* wpk;       // nchunk blocks of N x KC (K-major core matrices)
-  int N, nchunk, cout;   // N = pad16(cout)
-  const float* bias;     // (cout) or null
-  int H, W, npix;
+// periodic images of interior coordinate y in padded coordinates
+__device__ __forceinline__ int images(int y, int n, int* out) {
+  int k = 0;
+  out[k++] = y + PAD;
+  if (y < PAD) out[k++] = y + PAD + n;
+  else if (y >= n - PAD) out[k++] = y + PAD - n;
+  return k;
+}
+
+// store 8 channels (16 bytes) of pixel (b, y, x) and its halo copies
+__device__ __forceinline__ void store_px16(bf16* buf, int C, const Img& g, int b, int y, int x, int c0, uint4 v) {
+  int ys[2], xs[2];
+  const int ny = images(y, g.H, ys), nx = images(x, g.W, xs);
+  for (int i = 0; i < ny; i++)
+    for (int j = 0; j < nx; j++) *reinterpret_cast<uint4*>(buf + g.pix(b, ys[i], xs[j]) * C + c0) = v;
+}
+__device__ __forceinline__ void store_px1(bf16* buf, int C, const Img& g, int b, int y, int x, int c, bf16 v) {
+  int ys[2], xs[2];
+  const int ny = images(y, g.H, ys), nx = images(x, g.W, xs);
+  for (int i = 0; i < ny; i++)
+    for (int j = 0; j < nx; j++) buf[g.pix(b, ys[i], xs[j]) * C + c] = v;
+}
+
+__device__ __forceinline__ uint32_t tmem_cols(int n) {
+  return n <= 32 ? 32u : (n <= 64 ? 64u : (n <= 128 ? 128u : 256u));
+}
+
+__device__ __forceinline__ uint32_t bf2(float a, float b) {
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
+         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
+}
+
+// epilogue shared by the convolution kernels: 8 accumulator columns n0.. of
+// output pixel (b, y, x)
+struct Epi {
   int mode;              // 0: bias+ReLU -> out_bf; 1: affine -> out (NCHW); 2: ReLU mask -> out_bf
-  bf16* out_bf;          // NHWC, cout channels (cout multiple of 8)
-  void* out;             // NCHW float or double
+  int cout;              // real output channels (multiple of 8 in modes 0 and 2)
+  const float* bias;     // (cout) or null
+  bf16* out_bf;          // padded NHWC, cout channels
+  void* out;             // NCHW float or double, unpadded
   int out_f64;
   const float* oscale;   // mode 1: out = (acc + bias) * oscale + oshift
   const float* oshift;
-  const bf16* mask;      // mode 2: NHWC, cout channels
+  const bf16* mask;      // mode 2: padded NHWC, cout channels
+};
+
+__device__ __forceinline__ void epilogue8(const Epi& e, const Img& g, int b, int y, int x, int n0, const float* v) {
+  if (n0 >= e.cout) return;
+  if (e.mode == 0 || e.mode == 2) {
+    float t[8];
+    uint4 mk = make_uint4(0, 0, 0, 0);
+    if (e.mode == 2) mk = __ldg(reinterpret_cast<const uint4*>(e.mask + g.pix(b, y + PAD, x + PAD) * e.cout + n0));
+    const unsigned short* mh = reinterpret_cast<const unsigned short*>(&mk);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if (e.mode == 0) {
+        const float s = v[j] + e.bias[n0 + j];
+        t[j] = s > 0.f ? s : 0.f;
+      } else {
+        // ReLU derivative from the saved (post-ReLU) activation: positive BF16
+        const bool pos = (mh[j] & 0x8000u) == 0 && mh[j] != 0;
+        t[j] = pos ? v[j] : 0.f;
+      }
+    }
+    store_px16(e.out_bf, e.cout, g, b, y, x, n0, make_uint4(bf2(t[0], t[1]), bf2(t[2], t[3]), bf2(t[4], t[5]),
+                                                            bf2(t[6], t[7])));
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int n = n0 + j;
+      if (n < e.cout) {
+        const float t = (v[j] + (e.bias ? e.bias[n] : 0.f)) * e.oscale[n] + e.oshift[n];
+        const size_t o = (((size_t)b * e.cout + n) * g.H + y) * g.W + x;
+        if (e.out_f64) static_cast<double*>(e.out)[o] = (double)t;
+        else static_cast<float*>(e.out)[o] = t;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// halo-tile convolution (input channels a multiple of 16)
+// ---------------------------------------------------------------------------
+struct HaloArgs {
+  int cin;               // input channels
+  const bf16* wpk;       // 25 per-tap blocks of N x cin (K-major core matrices)
+  int N;                 // pad16(cout); SX * N <= 256
+  int tiles_x;           // W / (8 SX)
+  Img g;
+  Epi e;
   int* err;
 };
 
-__device__ __forceinline__ uint32_t tmem_cols(int N) { return N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u)); }
+template <int SX>
+__global__ void __launch_bounds__(128) k_conv_halo(const __grid_constant__ CUtensorMap tmap, HaloArgs a) {
+  constexpr int TXH = 8 * SX + 2 * PAD;
+  constexpr int SLAB = TXH * TYH * 16;     // bytes per 8 channels
+  extern __shared__ __align__(1024) unsigned char csm[];
+  __shared__ __align__(8) uint64_t bar_h, bar_done, bar_w[NST], bar_c[NST];
+  __shared__ uint32_t tslot;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int N = a.N, cin = a.cin, groups = cin / 8;
+  unsigned char* halo = csm;
+  unsigned char* wst = csm + (size_t)groups * SLAB;
+  const uint32_t wbytes = (uint32_t)N * cin * 2;
+  const int per_img = (a.g.H / TY) * a.tiles_x;
+  const int b = blockIdx.x / per_img, r = blockIdx.x - b * per_img;
+  const int y0 = (r / a.tiles_x) * TY, x0 = (r % a.tiles_x) * 8 * SX;
+  const uint32_t ncols = tmem_cols(SX * N);
+  if (warp == 0) tc::tmem_alloc(&tslot, ncols);
+  if (tid == 0) {
+    tc::mbar_init(&bar_h, 1);
+    tc::mbar_init(&bar_done, 1);
+    for (int s = 0; s < NST; s++) {
+      tc::mbar_init(&bar_w[s], 1);
+      tc::mbar_init(&bar_c[s], 1);
+    }
+    tc::mbar_fence_init();
+    s_fail = 0;
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_bf16(TM, N);
+    tc::mbar_expect_tx(&bar_h, (uint32_t)groups * SLAB);
+    for (int gq = 0; gq < groups; gq++) tc::tma_load_4d(halo + (size_t)gq * SLAB, &tmap, 8 * gq, x0, y0, b, &bar_h);
+    for (int s = 0; s < NST; s++) {
+      tc::mbar_expect_tx(&bar_w[s], wbytes);
+      tc::bulk_load(wst + (size_t)s * wbytes, a.wpk + (size_t)s * N * cin, wbytes, &bar_w[s]);
+    }
+    bool ok = tc::mbar_wait(&bar_h, 0);
+    const uint32_t hb = tc::smem_u32(halo), wb = tc::smem_u32(wst);
+    for (int t = 0; t < NTAP && ok; t++) {
+      const int s = t % NST;
+      ok = tc::mbar_wait(&bar_w[s], (t / NST) & 1);
+      if (!ok) break;
+      tc::fence_after();
+      const int dy = t / 5, dx = t - 5 * (t / 5);
+      for (int sx = 0; sx < SX; sx++) {
+        const uint32_t a0 = hb + (uint32_t)((dy * TXH + 8 * sx + dx) * 16);
+        for (int kk = 0; kk < cin / 16; kk++) {
+          const uint64_t ad = tc::sdesc(a0 + (uint32_t)(2 * kk) * SLAB, SLAB, TXH * 16);
+          const uint64_t bd = tc::sdesc(wb + (uint32_t)s * wbytes + kk * 256, 128, cin * 16);
+          tc::mma_bf16(tmem + sx * N, ad, bd, idesc, (t | kk) ? 1u : 0u);
+        }
+      }
+      tc::mma_commit(&bar_c[s]);
+      // refill the stage of tap t-1 (its MMAs precede tap t's in the pipe)
+      const int tp = t - 1;
+      if (tp >= 0 && tp + NST < NTAP) {
+        const int sp = tp % NST;
+        ok = tc::mbar_wait(&bar_c[sp], (tp / NST) & 1);
+        if (!ok) break;
+        tc::mbar_expect_tx(&bar_w[sp], wbytes);
+        tc::bulk_load(wst + (size_t)sp * wbytes, a.wpk + (size_t)(tp + NST) * N * cin, wbytes, &bar_w[sp]);
+      }
+    }
+    tc::mma_commit(&bar_done);
+    if (!ok) s_fail = 1;
+  }
+  const bool done = tc::mbar_wait(&bar_done, 0);
+  const bool failed = __syncthreads_or(!done) || s_fail;
+  if (failed) {
+    if (tid == 0) {
+      atomicExch(a.err, 1);
+      // bounded waits for copies still in flight before the CTA exits
+      tc::mbar_wait(&bar_h, 0, 10000000ull);
+      for (int s = 0; s < NST; s++) tc::mbar_wait(&bar_w[s], 0, 10000000ull);
+    }
+    __syncthreads();
+  } else {
+    tc::fence_after();
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    const int y = y0 + 4 * warp + (lane >> 3);
+    for (int sx = 0; sx < SX; sx++) {
+      const int x = x0 + 8 * sx + (lane & 7);
+      for (int n0 = 0; n0 < N; n0 += 8) {
+        float v[8];
+        tc::tmem_ld8(trow + sx * N + n0, v);
+        epilogue8(a.e, a.g, b, y, x, n0, v);
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
 
-template <bool VEC>
-__global__ void __launch_bounds__(128) k_conv(ConvArgs a) {
+// ---------------------------------------------------------------------------
+// gather convolution (few input channels): K chunks of 64 (tap, channel)
+// ---------------------------------------------------------------------------
+struct GatherArgs {
+  const bf16* in;        // padded NHWC, cin channels
+  int cin;
+  const bf16* wpk;       // nchunk blocks of N x KC
+  int N, nchunk;
+  int npix;
+  Img g;
+  Epi e;
+  int* err;
+};
+
+__global__ void __launch_bounds__(128) k_conv_gather(GatherArgs a) {
   extern __shared__ __align__(1024) unsigned char csm[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
@@ -107,11 +309,9 @@ __global__ void __launch_bounds__(128) k_conv(ConvArgs a) {
   tc::fence_after();
   const uint32_t tmem = tslot;
   const uint32_t idesc = tc::idesc_bf16(TM, N);
-
   const int p = blockIdx.x * TM + tid;           // this thread's pixel (tile row)
-  const int HW = a.H * a.W;
-  const int b = p / HW, rem = p - b * HW, y = rem / a.W, x = rem - (rem / a.W) * a.W;
-  const bf16* img = a.in + (size_t)b * HW * a.cin;
+  const int HW = a.g.H * a.g.W;
+  const int b = p / HW, rem = p - b * HW, y = rem / a.g.W, x = rem - (rem / a.g.W) * a.g.W;
   bool failed = false;
   for (int c = 0; c < a.nchunk; c++) {
     const int s = c & 1;
@@ -121,40 +321,21 @@ __global__ void __launch_bounds__(128) k_conv(ConvArgs a) {
     }
     unsigned char* sA = sA0 + s * CHUNK_A;
     unsigned char* sB = sB0 + s * bbytes;
-    if (VEC) {
-#pragma unroll
-      for (int g = 0; g < KC / 8; g++) {
-        const int k0 = c * KC + g * 8;
-        const int tap = k0 / a.cin, ci0 = k0 - tap * a.cin;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (tap < NTAP) {
-          const int yy = wrap(y + tap / 5 - 2, a.H), xx = wrap(x + tap % 5 - 2, a.W);
-          v = __ldg(reinterpret_cast<const uint4*>(img + ((size_t)yy * a.W + xx) * a.cin + ci0));
-        }
-        *reinterpret_cast<uint4*>(sA + tc::kmajor_off(tid, g * 8, KC)) = v;
-      }
-    } else {
 #pragma unroll 1
-      for (int g = 0; g < KC / 8; g++) {
-        unsigned short h[8];
+    for (int gq = 0; gq < KC / 8; gq++) {
+      unsigned short u[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const int k = c * KC + g * 8 + j;
-          const int tap = k / a.cin, ci = k - tap * a.cin;
-          unsigned short val = 0;
-          if (tap < NTAP) {
-            const int yy = wrap(y + tap / 5 - 2, a.H), xx = wrap(x + tap % 5 - 2, a.W);
-            val = __ldg(reinterpret_cast<const unsigned short*>(img + ((size_t)yy * a.W + xx) * a.cin + ci));
-          }
-          h[j] = val;
-        }
-        uint4 v;
-        v.x = h[0] | ((uint32_t)h[1] << 16);
-        v.y = h[2] | ((uint32_t)h[3] << 16);
-        v.z = h[4] | ((uint32_t)h[5] << 16);
-        v.w = h[6] | ((uint32_t)h[7] << 16);
-        *reinterpret_cast<uint4*>(sA + tc::kmajor_off(tid, g * 8, KC)) = v;
+      for (int j = 0; j < 8; j++) {
+        const int k = c * KC + gq * 8 + j;
+        const int tap = k / a.cin, ci = k - tap * a.cin;
+        unsigned short val = 0;
+        if (tap < NTAP)
+          val = __ldg(reinterpret_cast<const unsigned short*>(a.in + a.g.pix(b, y + tap / 5, x + tap % 5) * a.cin + ci));
+        u[j] = val;
       }
+      const uint4 v = make_uint4(u[0] | ((uint32_t)u[1] << 16), u[2] | ((uint32_t)u[3] << 16),
+                                 u[4] | ((uint32_t)u[5] << 16), u[6] | ((uint32_t)u[7] << 16));
+      *reinterpret_cast<uint4*>(sA + tc::kmajor_off(tid, gq * 8, KC)) = v;
     }
     const uint4* src = reinterpret_cast<const uint4*>(a.wpk + (size_t)c * N * KC);
     for (int i = tid; i < N * KC / 8; i += TM) reinterpret_cast<uint4*>(sB)[i] = __ldg(src + i);
@@ -177,7 +358,6 @@ __global__ void __launch_bounds__(128) k_conv(ConvArgs a) {
   }
   if (failed) {
     if (tid == 0) atomicExch(a.err, 1);
-    // give any MMA still in flight a bounded time to finish before freeing TMEM
     tc::mbar_wait(&mbar[0], 0, 10000000ull);
     tc::mbar_wait(&mbar[1], 0, 10000000ull);
   } else {
@@ -186,43 +366,7 @@ __global__ void __launch_bounds__(128) k_conv(ConvArgs a) {
     for (int n0 = 0; n0 < N; n0 += 8) {
       float v[8];
       tc::tmem_ld8(trow + n0, v);
-      if (n0 >= a.cout) continue;
-      if (a.mode == 0 || a.mode == 2) {
-        unsigned short h[8];
-        uint4 mk = make_uint4(0, 0, 0, 0);
-        if (a.mode == 2) mk = __ldg(reinterpret_cast<const uint4*>(a.mask + (size_t)p * a.cout + n0));
-        const unsigned short* mh = reinterpret_cast<const unsigned short*>(&mk);
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          float t = v[j];
-          if (a.mode == 0) {
-            t += a.bias[n0 + j];
-            t = t > 0.f ? t : 0.f;
-          } else {
-            // ReLU derivative of the saved activation (positive BF16: sign bit clear, nonzero)
-            const bool pos = (mh[j] & 0x8000u) == 0 && mh[j] != 0;
-            t = pos ? t : 0.f;
-          }
-          h[j] = __bfloat16_as_ushort(__float2bfloat16_rn(t));
-        }
-        uint4 o;
-        o.x = h[0] | ((uint32_t)h[1] << 16);
-        o.y = h[2] | ((uint32_t)h[3] << 16);
-        o.z = h[4] | ((uint32_t)h[5] << 16);
-        o.w = h[6] | ((uint32_t)h[7] << 16);
-        *reinterpret_cast<uint4*>(a.out_bf + (size_t)p * a.cout + n0) = o;
-      } else {
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const int n = n0 + j;
-          if (n < a.cout) {
-            const float t = (v[j] + (a.bias ? a.bias[n] : 0.f)) * a.oscale[n] + a.oshift[n];
-            const size_t o = (((size_t)b * a.cout + n) * a.H + y) * a.W + x;
-            if (a.out_f64) static_cast<double*>(a.out)[o] = (double)t;
-            else static_cast<float*>(a.out)[o] = t;
-          }
-        }
-      }
+      epilogue8(a.e, a.g, b, y, x, n0, v);
     }
   }
   tc::fence_before();
@@ -236,11 +380,12 @@ __global__ void __launch_bounds__(128) k_conv(ConvArgs a) {
 // image rows and adds its partial sums atomically into dw[co][tap][ci].
 // ---------------------------------------------------------------------------
 struct WgradArgs {
-  const bf16* x;   // layer input NHWC (cin)
+  const bf16* x;   // layer input, padded NHWC (cin)
   int cin;
-  const bf16* g;   // gradient of the pre-activation output NHWC (cout)
+  const bf16* g;   // gradient of the pre-activation output, padded NHWC (cout)
   int cout, N, M;  // N = pad16(cout), M = 25 cin
-  int H, W, nrows, rows_per_cta;
+  Img gm;
+  int nrows, rows_per_cta;
   float* dw;
   int* err;
 };
@@ -281,19 +426,16 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
     unsigned char* sA = sA0 + s * CHUNK_A;
     unsigned char* sB = sB0 + s * bbytes;
     const int rr = r0 + c;
-    const int b = rr / a.H, y = rr - (rr / a.H) * a.H;
-    const bf16* img = a.x + (size_t)b * a.H * a.W * a.cin;
-    // A[m][k] = x[b][y + dy][k + dx][ci]
+    const int b = rr / a.gm.H, y = rr - (rr / a.gm.H) * a.gm.H;
+    // A[m][k] = x[b][y + dy][k + dx][ci] (padded coordinates)
     if (VECX) {
       const int k = tid & 63;
       for (int mg = tid >> 6; mg < TM / 8; mg += 2) {
         const int m = m0 + mg * 8;
         const int tap = m / a.cin, ci0 = m - tap * a.cin;
         uint4 v = make_uint4(0, 0, 0, 0);
-        if (tap < NTAP) {
-          const int yy = wrap(y + tap / 5 - 2, a.H), xx = wrap(k + tap % 5 - 2, a.W);
-          v = __ldg(reinterpret_cast<const uint4*>(img + ((size_t)yy * a.W + xx) * a.cin + ci0));
-        }
+        if (tap < NTAP)
+          v = __ldg(reinterpret_cast<const uint4*>(a.x + a.gm.pix(b, y + tap / 5, k + tap % 5) * a.cin + ci0));
         const unsigned short* h = reinterpret_cast<const unsigned short*>(&v);
 #pragma unroll
         for (int j = 0; j < 8; j++)
@@ -301,19 +443,17 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
       }
     } else {
       for (int i = tid; i < TM * KC; i += TM) {
-        const int k = i & 63, r = i >> 6;
-        const int m = m0 + r;
+        const int k = i & 63, rw = i >> 6;
+        const int m = m0 + rw;
         const int tap = m / a.cin, ci = m - tap * a.cin;
         unsigned short val = 0;
-        if (tap < NTAP) {
-          const int yy = wrap(y + tap / 5 - 2, a.H), xx = wrap(k + tap % 5 - 2, a.W);
-          val = __ldg(reinterpret_cast<const unsigned short*>(img + ((size_t)yy * a.W + xx) * a.cin + ci));
-        }
-        *reinterpret_cast<unsigned short*>(sA + tc::kmajor_off(r, k, KC)) = val;
+        if (tap < NTAP)
+          val = __ldg(reinterpret_cast<const unsigned short*>(a.x + a.gm.pix(b, y + tap / 5, k + tap % 5) * a.cin + ci));
+        *reinterpret_cast<unsigned short*>(sA + tc::kmajor_off(rw, k, KC)) = val;
       }
     }
     // B[n][k] = g[b][y][k][n]
-    const bf16* grow = a.g + ((size_t)rr * a.W) * a.cout;
+    const bf16* grow = a.g + a.gm.pix(b, y + PAD, PAD) * a.cout;
     if (VECG) {
       for (int i = tid; i < (N / 8) * KC; i += TM) {
         const int k = i & 63, ng = i >> 6;
@@ -375,23 +515,24 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
 // ---------------------------------------------------------------------------
 // small kernels: layout conversion, packing, loss, bias gradient, Adam
 // ---------------------------------------------------------------------------
-// NCHW (float or double) -> NHWC BF16 with (x - mean[c]) * inv_std[c]
+// NCHW (float or double) -> padded NHWC BF16 with (x - mean[c]) * inv_std[c]
 template <class T>
-__global__ void k_to_nhwc(const T* __restrict__ x, bf16* __restrict__ out, int B, int C, int HW,
+__global__ void k_to_nhwc(const T* __restrict__ x, bf16* __restrict__ out, int B, int C, Img g,
                           const float* __restrict__ mean, const float* __restrict__ inv_std) {
+  const int HW = g.H * g.W;
   const size_t n = (size_t)B * C * HW;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % C);
     const size_t pix = i / C;
-    const size_t b = pix / HW, hw = pix - b * HW;
-    const float v = (float)x[(b * C + c) * HW + hw];
-    out[i] = __float2bfloat16_rn((v - mean[c]) * inv_std[c]);
+    const int b = (int)(pix / HW), hw = (int)(pix - (size_t)b * HW);
+    const float v = (float)x[((size_t)b * C + c) * HW + hw];
+    store_px1(out, C, g, b, hw / g.W, hw % g.W, c, __float2bfloat16_rn((v - mean[c]) * inv_std[c]));
   }
 }
 
-// packed weights: forward (transpose = 0) or dgrad (transpose = 1)
-__global__ void k_pack(const float* __restrict__ w, int cin, int cout, int transpose, bf16* __restrict__ out,
-                       int N, int nchunk) {
+// chunked packing for the gather kernel: forward (transpose = 0) or dgrad
+__global__ void k_pack_chunks(const float* __restrict__ w, int cin, int cout, int transpose, bf16* __restrict__ out,
+                              int N, int nchunk) {
   const int kin = transpose ? cout : cin;      // channels along K
   const int nreal = transpose ? cin : cout;    // real columns
   const size_t total = (size_t)nchunk * N * KC;
@@ -406,38 +547,62 @@ __global__ void k_pack(const float* __restrict__ w, int cin, int cout, int trans
       if (!transpose) v = w[((size_t)n * NTAP + tap) * cin + ch];
       else v = w[((size_t)ch * NTAP + (NTAP - 1 - tap)) * cin + n];
     }
-    const size_t o = (size_t)c * N * KC + tc::kmajor_off(n, kk, KC) / 2;
-    out[o] = __float2bfloat16_rn(v);
+    out[(size_t)c * N * KC + tc::kmajor_off(n, kk, KC) / 2] = __float2bfloat16_rn(v);
   }
 }
 
-// MSE loss of y (NCHW FP32) against t; gradient 2 (y - t) / count as NHWC BF16
+// per-tap packing for the halo kernel: 25 blocks of N x kin
+__global__ void k_pack_taps(const float* __restrict__ w, int cin, int cout, int transpose, bf16* __restrict__ out,
+                            int N) {
+  const int kin = transpose ? cout : cin;
+  const int nreal = transpose ? cin : cout;
+  const size_t total = (size_t)NTAP * N * kin;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int tap = (int)(i / ((size_t)N * kin));
+    const int rem = (int)(i - (size_t)tap * N * kin);
+    const int n = rem / kin, ch = rem - n * kin;
+    float v = 0.f;
+    if (n < nreal) {
+      if (!transpose) v = w[((size_t)n * NTAP + tap) * cin + ch];
+      else v = w[((size_t)ch * NTAP + (NTAP - 1 - tap)) * cin + n];
+    }
+    out[(size_t)tap * N * kin + tc::kmajor_off(n, ch, kin) / 2] = __float2bfloat16_rn(v);
+  }
+}
+
+// MSE loss of y (NCHW FP32) against t; gradient 2 (y - t) / count as padded
+// NHWC BF16
 __global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, bf16* __restrict__ g, int B, int C,
-                      int HW, float* __restrict__ loss_sum) {
+                      Img gm, float* __restrict__ loss_sum) {
+  const int HW = gm.H * gm.W;
   const size_t n = (size_t)B * C * HW;
   const float sc = 2.f / (float)n;
   float acc = 0.f;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const size_t b = i / ((size_t)C * HW);
-    const size_t r = i - b * C * HW;
-    const int c = (int)(r / HW);
-    const size_t hw = r - (size_t)c * HW;
+    const int b = (int)(i / ((size_t)C * HW));
+    const int r = (int)(i - (size_t)b * C * HW);
+    const int c = r / HW, hw = r - c * HW;
     const float d = y[i] - t[i];
     acc += d * d;
-    g[(b * HW + hw) * C + c] = __float2bfloat16_rn(sc * d);
+    store_px1(g, C, gm, b, hw / gm.W, hw % gm.W, c, __float2bfloat16_rn(sc * d));
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, acc / (float)n);
 }
 
-// db[c] += sum over pixels of g[p][c]
-__global__ void k_bias_grad(const bf16* __restrict__ g, int npix, int C, float* __restrict__ db) {
+// db[c] += sum over interior pixels of g[p][c]
+__global__ void k_bias_grad(const bf16* __restrict__ g, int B, int C, Img gm, float* __restrict__ db) {
   __shared__ float acc[128];
   for (int i = threadIdx.x; i < C; i += blockDim.x) acc[i] = 0.f;
   __syncthreads();
-  const size_t n = (size_t)npix * C;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    atomicAdd(&acc[i % C], __bfloat162float(g[i]));
+  const int HW = gm.H * gm.W;
+  const size_t n = (size_t)B * HW * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const size_t pix = i / C;
+    const int b = (int)(pix / HW), hw = (int)(pix - (size_t)b * HW);
+    atomicAdd(&acc[c], __bfloat162float(g[gm.pix(b, hw / gm.W + PAD, hw % gm.W + PAD) * C + c]));
+  }
   __syncthreads();
   for (int i = threadIdx.x; i < C; i += blockDim.x) atomicAdd(&db[i], acc[i]);
 }
@@ -454,30 +619,41 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
   }
 }
 
+// one convolution direction of a layer: packed weights and kernel choice
+struct ConvPlan {
+  int kin = 0, nout = 0;   // channels along K (input) and real output channels
+  int N = 0;               // pad16(nout)
+  bool halo = false;       // halo kernel (kin % 16 == 0) or gather kernel
+  int sx = 0;              // halo kernel tile width / 8
+  int nchunk = 0;          // gather kernel K chunks
+  bf16* w = nullptr;
+  size_t smem = 0;
+};
+
 struct CnnLayer {
   int cin, cout;
-  int Nf, nchf;      // forward packing
-  int Nd, nchd;      // dgrad packing
-  size_t woff, boff; // offsets into the parameter vector
-  bf16* wf;
-  bf16* wd;
+  ConvPlan fwd, bwd;
+  size_t woff, boff;   // offsets into the parameter vector
 };
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
 }  // namespace
 
 struct pqg_cnn {
   int nl = 0, H = 0, W = 0, maxB = 0;
+  Img g{};
   std::vector<CnnLayer> L;
   size_t nparams = 0;
   float* params = nullptr;
   float* grads = nullptr;
   float* m = nullptr;
   float* v = nullptr;
-  std::vector<bf16*> act;     // act[0] input, act[l] output of layer l-1 (post-ReLU)
+  std::vector<bf16*> act;     // act[0] input, act[l] output of layer l-1 (post-ReLU); padded NHWC
   float* out = nullptr;       // last layer, NCHW FP32 (training)
-  bf16* ga = nullptr;
+  bf16* ga = nullptr;         // gradient ping-pong buffers, padded NHWC
   bf16* gb = nullptr;
-  float* norm = nullptr;      // in_mean, in_inv_std, out_scale, out_shift, id_scale(1), id_shift(0)
+  float* norm = nullptr;      // in_mean, in_inv_std, out_scale, out_shift, ones, zeros (128 each)
   int cmax = 0;
   float* loss = nullptr;
   int* err = nullptr;
@@ -486,34 +662,100 @@ struct pqg_cnn {
 
 namespace {
 
-size_t conv_smem(int N) { return 2 * (size_t)CHUNK_A + 2 * (size_t)N * KC * 2; }
+size_t gather_smem(int N) { return 2 * (size_t)CHUNK_A + 2 * (size_t)N * KC * 2; }
 
-int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int batch, int mode, bf16* out_bf,
-                void* out, int out_f64, const float* oscale, const float* oshift, const bf16* mask,
+size_t halo_smem(int sx, int kin, int N) {
+  const size_t slab = (size_t)(8 * sx + 2 * PAD) * TYH * 16;
+  return (size_t)(kin / 8) * slab + (size_t)NST * N * kin * 2;
+}
+
+void plan_conv(ConvPlan& c, int W, int kin, int nout) {
+  c.kin = kin;
+  c.nout = nout;
+  c.N = pad16(nout);
+  c.halo = kin % 16 == 0;
+  c.nchunk = (NTAP * kin + KC - 1) / KC;
+  if (c.halo) {
+    // widest tile within 256 TMEM columns and about 110 KiB of shared memory
+    // (two CTAs per SM), else the widest that fits at all; PQG_CNN_SX caps
+    // the width (tuning)
+    int cap = 4;
+    if (const char* e = getenv("PQG_CNN_SX")) cap = std::max(1, atoi(e));
+    c.sx = 0;
+    for (int sx : {4, 2, 1}) {
+      if (sx > cap) continue;
+      if ((W % (8 * sx)) || sx * c.N > 256) continue;
+      if (halo_smem(sx, kin, c.N) <= 110 * 1024) { c.sx = sx; break; }
+    }
+    if (!c.sx)
+      for (int sx : {2, 1})
+        if (sx <= cap && !(W % (8 * sx)) && sx * c.N <= 256 && halo_smem(sx, kin, c.N) <= 200 * 1024) {
+          c.sx = sx;
+          break;
+        }
+    if (!c.sx) c.halo = false;
+  }
+  c.smem = c.halo ? halo_smem(c.sx, kin, c.N) : gather_smem(c.N);
+}
+
+size_t plan_weight_elems(const ConvPlan& c) {
+  return c.halo ? (size_t)NTAP * c.N * c.kin : (size_t)c.nchunk * c.N * KC;
+}
+
+int encode_map(CUtensorMap* m, const bf16* buf, int C, const pqg_cnn* net, int sx) {
+  if (!g_encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return cfail(PQG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)net->g.Wp, (cuuint64_t)net->g.Hp, (cuuint64_t)net->maxB};
+  cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)net->g.Wp * C * 2, (cuuint64_t)net->g.Hp * net->g.Wp * C * 2};
+  cuuint32_t box[4] = {8, (cuuint32_t)(8 * sx + 2 * PAD), (cuuint32_t)TYH, 1};
+  cuuint32_t es[4] = {1, 1, 1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(buf), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cfail(PQG_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return PQG_OK;
+}
+
+int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int batch, const Epi& e,
                 cudaStream_t st) {
-  ConvArgs a;
-  a.in = in;
-  a.cin = dgrad ? l.cout : l.cin;
-  a.wpk = dgrad ? l.wd : l.wf;
-  a.N = dgrad ? l.Nd : l.Nf;
-  a.nchunk = dgrad ? l.nchd : l.nchf;
-  a.cout = dgrad ? l.cin : l.cout;
-  a.bias = dgrad ? nullptr : net->params + l.boff;
-  a.H = net->H;
-  a.W = net->W;
-  a.npix = batch * net->H * net->W;
-  a.mode = mode;
-  a.out_bf = out_bf;
-  a.out = out;
-  a.out_f64 = out_f64;
-  a.oscale = oscale;
-  a.oshift = oshift;
-  a.mask = mask;
-  a.err = net->err;
-  const size_t smem = conv_smem(a.N);
-  const dim3 grid(a.npix / TM);
-  if (a.cin % 8 == 0) k_conv<true><<<grid, TM, smem, st>>>(a);
-  else k_conv<false><<<grid, TM, smem, st>>>(a);
+  const ConvPlan& c = dgrad ? l.bwd : l.fwd;
+  if (c.halo) {
+    CUtensorMap m;
+    int rc = encode_map(&m, in, c.kin, net, c.sx);
+    if (rc) return rc;
+    HaloArgs a;
+    a.cin = c.kin;
+    a.wpk = c.w;
+    a.N = c.N;
+    a.tiles_x = net->W / (8 * c.sx);
+    a.g = net->g;
+    a.e = e;
+    a.err = net->err;
+    const dim3 grid(batch * (net->H / TY) * a.tiles_x);
+    switch (c.sx) {
+      case 4: k_conv_halo<4><<<grid, TM, c.smem, st>>>(m, a); break;
+      case 2: k_conv_halo<2><<<grid, TM, c.smem, st>>>(m, a); break;
+      default: k_conv_halo<1><<<grid, TM, c.smem, st>>>(m, a); break;
+    }
+  } else {
+    GatherArgs a;
+    a.in = in;
+    a.cin = c.kin;
+    a.wpk = c.w;
+    a.N = c.N;
+    a.nchunk = c.nchunk;
+    a.npix = batch * net->H * net->W;
+    a.g = net->g;
+    a.e = e;
+    a.err = net->err;
+    k_conv_gather<<<a.npix / TM, TM, c.smem, st>>>(a);
+  }
   CCUDA(cudaGetLastError());
   return PQG_OK;
 }
@@ -524,10 +766,9 @@ int launch_wgrad(pqg_cnn* net, const CnnLayer& l, const bf16* x, const bf16* g, 
   a.cin = l.cin;
   a.g = g;
   a.cout = l.cout;
-  a.N = l.Nf;
+  a.N = pad16(l.cout);
   a.M = NTAP * l.cin;
-  a.H = net->H;
-  a.W = net->W;
+  a.gm = net->g;
   a.nrows = batch * net->H;
   const int mt = (a.M + TM - 1) / TM;
   const int target = 4 * 152;
@@ -536,7 +777,7 @@ int launch_wgrad(pqg_cnn* net, const CnnLayer& l, const bf16* x, const bf16* g, 
   ks = (a.nrows + a.rows_per_cta - 1) / a.rows_per_cta;
   a.dw = net->grads + l.woff;
   a.err = net->err;
-  const size_t smem = conv_smem(a.N);
+  const size_t smem = gather_smem(a.N);
   const dim3 grid(mt, ks);
   const bool vx = l.cin % 8 == 0, vg = l.cout % 8 == 0;
 #define WG(X, G) k_wgrad<X, G><<<grid, TM, smem, st>>>(a)
@@ -549,11 +790,17 @@ int launch_wgrad(pqg_cnn* net, const CnnLayer& l, const bf16* x, const bf16* g, 
   return PQG_OK;
 }
 
-// the largest tile (N = 128) needs 64 KiB of dynamic shared memory
+// dynamic shared memory limit of every kernel: the device's opt-in maximum
+// less room for the kernels' static shared memory
 int set_attrs() {
-  const int big = (int)conv_smem(128);
-  CCUDA(cudaFuncSetAttribute(k_conv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  CCUDA(cudaFuncSetAttribute(k_conv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  int dev = 0, optin = 0;
+  CCUDA(cudaGetDevice(&dev));
+  CCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const int big = optin - 2048;
+  CCUDA(cudaFuncSetAttribute(k_conv_halo<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_conv_halo<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_conv_halo<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(k_conv_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_wgrad<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_wgrad<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_wgrad<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -565,10 +812,14 @@ int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16)
 
 int repack(pqg_cnn* net, cudaStream_t st) {
   for (auto& l : net->L) {
-    k_pack<<<grid_for((size_t)l.nchf * l.Nf * KC), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, 0, l.wf, l.Nf,
-                                                               l.nchf);
-    k_pack<<<grid_for((size_t)l.nchd * l.Nd * KC), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, 1, l.wd, l.Nd,
-                                                               l.nchd);
+    for (int d = 0; d < 2; d++) {
+      const ConvPlan& c = d ? l.bwd : l.fwd;
+      if (c.halo)
+        k_pack_taps<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w, c.N);
+      else
+        k_pack_chunks<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w,
+                                                                     c.N, c.nchunk);
+    }
   }
   CCUDA(cudaGetLastError());
   return PQG_OK;
@@ -590,9 +841,20 @@ int forward_layers(pqg_cnn* net, int batch, void* out, int out_f64, const float*
                    cudaStream_t st) {
   for (int i = 0; i < net->nl; i++) {
     const CnnLayer& l = net->L[i];
-    const bool last = i == net->nl - 1;
-    int rc = launch_conv(net, l, false, net->act[i], batch, last ? 1 : 0, last ? nullptr : net->act[i + 1],
-                         last ? out : nullptr, out_f64, oscale, oshift, nullptr, st);
+    Epi e{};
+    e.cout = l.cout;
+    e.bias = net->params + l.boff;
+    if (i < net->nl - 1) {
+      e.mode = 0;
+      e.out_bf = net->act[i + 1];
+    } else {
+      e.mode = 1;
+      e.out = out;
+      e.out_f64 = out_f64;
+      e.oscale = oscale;
+      e.oshift = oshift;
+    }
+    int rc = launch_conv(net, l, false, net->act[i], batch, e, st);
     if (rc) return rc;
   }
   return PQG_OK;
@@ -607,8 +869,8 @@ PQG_API const char* pqg_cnn_last_error(void) { return c_last_error.c_str(); }
 PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int height, int width, int max_batch) {
   if (!out || !channels || nlayers < 1 || nlayers > 16) return cfail(PQG_ERR_INVALID, "bad layer count");
   if (width != KC) return cfail(PQG_ERR_UNSUPPORTED, "image width must be 64");
-  if (height < 5 || max_batch < 1 || ((size_t)height * width * max_batch) % TM)
-    return cfail(PQG_ERR_INVALID, "batch * height * width must be a multiple of 128");
+  if (height < TY || height % TY || max_batch < 1)
+    return cfail(PQG_ERR_UNSUPPORTED, "image height must be a positive multiple of 16");
   for (int i = 0; i <= nlayers; i++)
     if (channels[i] < 1 || channels[i] > 128) return cfail(PQG_ERR_UNSUPPORTED, "channels must be in 1..128");
   for (int i = 1; i < nlayers; i++)
@@ -618,15 +880,14 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
   net->H = height;
   net->W = width;
   net->maxB = max_batch;
+  net->g = Img{height, width, height + 2 * PAD, width + 2 * PAD};
   size_t off = 0;
   for (int i = 0; i < nlayers; i++) {
     CnnLayer l{};
     l.cin = channels[i];
     l.cout = channels[i + 1];
-    l.Nf = pad16(l.cout);
-    l.nchf = (NTAP * l.cin + KC - 1) / KC;
-    l.Nd = pad16(l.cin);
-    l.nchd = (NTAP * l.cout + KC - 1) / KC;
+    plan_conv(l.fwd, width, l.cin, l.cout);
+    plan_conv(l.bwd, width, l.cout, l.cin);
     l.woff = off;
     off += (size_t)l.cout * NTAP * l.cin;
     l.boff = off;
@@ -635,10 +896,11 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
     net->cmax = std::max(net->cmax, std::max(l.cin, l.cout));
   }
   net->nparams = off;
+  const size_t npad = (size_t)max_batch * net->g.Hp * net->g.Wp;
   const size_t npix = (size_t)max_batch * height * width;
   auto fail = [&](const char* what) {
     pqg_cnn_destroy(net);
-    return cfail(PQG_ERR_CUDA, std::string("allocation failed: ") + what);
+    return cfail(PQG_ERR_NOMEM, std::string("allocation failed: ") + what);
   };
   if (cudaMalloc(&net->params, 4 * off) || cudaMalloc(&net->grads, 4 * off) || cudaMalloc(&net->m, 4 * off) ||
       cudaMalloc(&net->v, 4 * off))
@@ -647,14 +909,14 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
   cudaMemset(net->m, 0, 4 * off);
   cudaMemset(net->v, 0, 4 * off);
   for (auto& l : net->L) {
-    if (cudaMalloc(&l.wf, (size_t)l.nchf * l.Nf * KC * 2) || cudaMalloc(&l.wd, (size_t)l.nchd * l.Nd * KC * 2))
+    if (cudaMalloc(&l.fwd.w, 2 * plan_weight_elems(l.fwd)) || cudaMalloc(&l.bwd.w, 2 * plan_weight_elems(l.bwd)))
       return fail("packed weights");
   }
   net->act.assign(nlayers, nullptr);
   for (int i = 0; i < nlayers; i++)
-    if (cudaMalloc(&net->act[i], npix * net->L[i].cin * 2)) return fail("activations");
-  if (cudaMalloc(&net->out, npix * net->L.back().cout * 4) || cudaMalloc(&net->ga, npix * net->cmax * 2) ||
-      cudaMalloc(&net->gb, npix * net->cmax * 2) || cudaMalloc(&net->norm, 4 * 6 * 128) ||
+    if (cudaMalloc(&net->act[i], npad * net->L[i].cin * 2)) return fail("activations");
+  if (cudaMalloc(&net->out, npix * net->L.back().cout * 4) || cudaMalloc(&net->ga, npad * net->cmax * 2) ||
+      cudaMalloc(&net->gb, npad * net->cmax * 2) || cudaMalloc(&net->norm, 4 * 6 * 128) ||
       cudaMalloc(&net->loss, 4) || cudaMalloc(&net->err, 4))
     return fail("buffers");
   std::vector<float> nm(6 * 128, 0.f);
@@ -665,7 +927,15 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
   }
   cudaMemcpy(net->norm, nm.data(), 4 * nm.size(), cudaMemcpyHostToDevice);
   cudaMemset(net->err, 0, 4);
-  if (set_attrs() != PQG_OK || cudaDeviceSynchronize() != cudaSuccess) return fail("initialisation");
+  if (set_attrs() != PQG_OK) {
+    const std::string msg = c_last_error;
+    pqg_cnn_destroy(net);
+    return cfail(PQG_ERR_CUDA, "initialisation failed: " + msg);
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    pqg_cnn_destroy(net);
+    return cfail(PQG_ERR_CUDA, "initialisation failed");
+  }
   *out = net;
   return PQG_OK;
 }
@@ -677,8 +947,8 @@ PQG_API int pqg_cnn_destroy(pqg_cnn* net) {
   cudaFree(net->m);
   cudaFree(net->v);
   for (auto& l : net->L) {
-    cudaFree(l.wf);
-    cudaFree(l.wd);
+    cudaFree(l.fwd.w);
+    cudaFree(l.bwd.w);
   }
   for (auto p : net->act) cudaFree(p);
   cudaFree(net->out);
@@ -762,55 +1032,56 @@ PQG_API int pqg_cnn_set_norm(pqg_cnn* net, const float* in_mean, const float* in
 // and y (batch, cout, H, W) are device arrays, FP32 or FP64.
 PQG_API int pqg_cnn_forward(pqg_cnn* net, const void* x, int x_f64, void* y, int y_f64, int batch, void* stream) {
   if (!net || !x || !y) return cfail(PQG_ERR_INVALID, "NULL argument");
-  if (batch < 1 || batch > net->maxB || ((size_t)batch * net->H * net->W) % TM)
-    return cfail(PQG_ERR_INVALID, "bad batch size");
+  if (batch < 1 || batch > net->maxB) return cfail(PQG_ERR_INVALID, "bad batch size");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t n = (size_t)batch * net->L[0].cin * net->H * net->W;
   if (x_f64)
-    k_to_nhwc<double><<<grid_for(n), 256, 0, st>>>((const double*)x, net->act[0], batch, net->L[0].cin,
-                                                   net->H * net->W, net->norm, net->norm + 128);
+    k_to_nhwc<double><<<grid_for(n), 256, 0, st>>>((const double*)x, net->act[0], batch, net->L[0].cin, net->g,
+                                                   net->norm, net->norm + 128);
   else
-    k_to_nhwc<float><<<grid_for(n), 256, 0, st>>>((const float*)x, net->act[0], batch, net->L[0].cin,
-                                                  net->H * net->W, net->norm, net->norm + 128);
+    k_to_nhwc<float><<<grid_for(n), 256, 0, st>>>((const float*)x, net->act[0], batch, net->L[0].cin, net->g,
+                                                  net->norm, net->norm + 128);
   CCUDA(cudaGetLastError());
-  int rc = forward_layers(net, batch, y, y_f64, net->norm + 256, net->norm + 384, st);
-  if (rc) return rc;
-  return PQG_OK;
+  return forward_layers(net, batch, y, y_f64, net->norm + 256, net->norm + 384, st);
 }
 
 // gradients of the MSE loss of net(x) against t (both standardised, FP32
 // NCHW device arrays) into the gradient vector; loss (host) if not NULL
 PQG_API int pqg_cnn_backward(pqg_cnn* net, const float* x, const float* t, int batch, float* loss, void* stream) {
   if (!net || !x || !t) return cfail(PQG_ERR_INVALID, "NULL argument");
-  if (batch < 1 || batch > net->maxB || ((size_t)batch * net->H * net->W) % TM)
-    return cfail(PQG_ERR_INVALID, "bad batch size");
+  if (batch < 1 || batch > net->maxB) return cfail(PQG_ERR_INVALID, "bad batch size");
   cudaStream_t st = (cudaStream_t)stream;
-  const int HW = net->H * net->W;
-  const size_t npix = (size_t)batch * HW;
-  const float* ident = net->norm + 512;   // 1 then 0 (norm + 640 holds zeros)
-  k_to_nhwc<float><<<grid_for(npix * net->L[0].cin), 256, 0, st>>>(x, net->act[0], batch, net->L[0].cin, HW,
-                                                                   net->norm + 640, ident);
+  const size_t npix = (size_t)batch * net->H * net->W;
+  const float* ones = net->norm + 512;
+  const float* zeros = net->norm + 640;
+  k_to_nhwc<float><<<grid_for(npix * net->L[0].cin), 256, 0, st>>>(x, net->act[0], batch, net->L[0].cin, net->g,
+                                                                   zeros, ones);
   CCUDA(cudaGetLastError());
-  int rc = forward_layers(net, batch, net->out, 0, ident, net->norm + 640, st);
+  int rc = forward_layers(net, batch, net->out, 0, ones, zeros, st);
   if (rc) return rc;
   CCUDA(cudaMemsetAsync(net->grads, 0, 4 * net->nparams, st));
   CCUDA(cudaMemsetAsync(net->loss, 0, 4, st));
   const int nl = net->nl;
   const int cl = net->L[nl - 1].cout;
-  k_mse<<<grid_for(npix * cl), 256, 0, st>>>(net->out, t, net->ga, batch, cl, HW, net->loss);
+  k_mse<<<grid_for(npix * cl), 256, 0, st>>>(net->out, t, net->ga, batch, cl, net->g, net->loss);
   CCUDA(cudaGetLastError());
   bf16* g = net->ga;     // gradient of the current layer's pre-activation output
   bf16* gn = net->gb;
   for (int i = nl - 1; i >= 0; i--) {
     const CnnLayer& l = net->L[i];
-    k_bias_grad<<<std::min<size_t>(1024, (npix * l.cout + 255) / 256), 256, 0, st>>>(g, (int)npix, l.cout,
-                                                                                  net->grads + l.boff);
+    k_bias_grad<<<(int)std::min<size_t>(1024, (npix * l.cout + 255) / 256), 256, 0, st>>>(
+        g, batch, l.cout, net->g, net->grads + l.boff);
     CCUDA(cudaGetLastError());
     rc = launch_wgrad(net, l, net->act[i], g, batch, st);
     if (rc) return rc;
     if (i > 0) {
       // gradient of layer i's input, masked by the ReLU of layer i-1's output
-      rc = launch_conv(net, l, true, g, batch, 2, gn, nullptr, 0, nullptr, nullptr, net->act[i], st);
+      Epi e{};
+      e.mode = 2;
+      e.cout = l.cin;
+      e.out_bf = gn;
+      e.mask = net->act[i];
+      rc = launch_conv(net, l, true, g, batch, e, st);
       if (rc) return rc;
       std::swap(g, gn);
     }
