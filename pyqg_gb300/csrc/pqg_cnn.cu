@@ -24,7 +24,8 @@
 //    pixel); the A operand of tap (dy, dx) is then a shifted descriptor over
 //    the same slabs (core matrix = 8 consecutive pixels of a row, next
 //    8-pixel group = next image row).  The per-tap weight blocks stream
-//    through a 3-stage bulk-copy pipeline; one thread issues the MMAs.
+//    through a bulk-copy ring of `nst` stages (all 25 taps resident when
+//    they fit); one thread issues the MMAs.
 //  * k_conv_gather (few input channels, e.g. the 2-channel input layer):
 //    threads gather a K-chunk of 64 (tap, channel) pairs per pixel.
 // The weight gradient gathers (tap, channel) x pixel tiles (k_wgrad) and
@@ -59,7 +60,7 @@ constexpr int PAD = 2;     // halo width
 constexpr int CHUNK_A = TM * KC * 2;   // bytes of one A stage (gather kernels)
 constexpr int TY = 16;     // output rows of a halo-kernel tile
 constexpr int TYH = TY + 2 * PAD;
-constexpr int NST = 3;     // weight stages of the halo kernel
+constexpr int MAXST = 2 * NTAP;   // weight stages of the halo kernel (at most one per tap and unit)
 
 thread_local std::string c_last_error;
 
@@ -106,8 +107,9 @@ __device__ __forceinline__ void store_px1(bf16* buf, int C, const Img& g, int b,
     for (int j = 0; j < nx; j++) buf[g.pix(b, ys[i], xs[j]) * C + c] = v;
 }
 
+// TMEM allocation: a power of two of at least 32 columns (n <= 512)
 __device__ __forceinline__ uint32_t tmem_cols(int n) {
-  return n <= 32 ? 32u : (n <= 64 ? 64u : (n <= 128 ? 128u : 256u));
+  return n <= 32 ? 32u : (n <= 64 ? 64u : (n <= 128 ? 128u : (n <= 256 ? 256u : 512u)));
 }
 
 __device__ __forceinline__ uint32_t bf2(float a, float b) {
@@ -129,7 +131,9 @@ struct Epi {
   const bf16* mask;      // mode 2: padded NHWC, cout channels
 };
 
-__device__ __forceinline__ void epilogue8(const Epi& e, const Img& g, int b, int y, int x, int n0, const float* v) {
+// `bias` is the bias vector (global or shared memory) or null
+__device__ __forceinline__ void epilogue8(const Epi& e, const float* bias, const Img& g, int b, int y, int x, int n0,
+                                          const float* v) {
   if (n0 >= e.cout) return;
   if (e.mode == 0 || e.mode == 2) {
     float t[8];
@@ -139,7 +143,7 @@ __device__ __forceinline__ void epilogue8(const Epi& e, const Img& g, int b, int
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       if (e.mode == 0) {
-        const float s = v[j] + e.bias[n0 + j];
+        const float s = v[j] + bias[n0 + j];
         t[j] = s > 0.f ? s : 0.f;
       } else {
         // ReLU derivative from the saved (post-ReLU) activation: positive BF16
@@ -154,7 +158,7 @@ __device__ __forceinline__ void epilogue8(const Epi& e, const Img& g, int b, int
     for (int j = 0; j < 8; j++) {
       const int n = n0 + j;
       if (n < e.cout) {
-        const float t = (v[j] + (e.bias ? e.bias[n] : 0.f)) * e.oscale[n] + e.oshift[n];
+        const float t = (v[j] + (bias ? bias[n] : 0.f)) * e.oscale[n] + e.oshift[n];
         const size_t o = (((size_t)b * e.cout + n) * g.H + y) * g.W + x;
         if (e.out_f64) static_cast<double*>(e.out)[o] = (double)t;
         else static_cast<float*>(e.out)[o] = t;
@@ -164,110 +168,203 @@ __device__ __forceinline__ void epilogue8(const Epi& e, const Img& g, int b, int
 }
 
 // ---------------------------------------------------------------------------
-// halo-tile convolution (input channels a multiple of 16)
+// halo-tile convolution (input channels 16, 32, 64 or 128), persistent and
+// warp-specialised, one CTA per SM, 5 + SX warps:
+//   warps 0-3     epilogue: TMEM -> registers -> global (warp w owns TMEM
+//                 lanes 32w..32w+31)
+//   warp 4        producer (one lane): TMA halo tiles into `nh` buffers,
+//                 per-tap weight blocks into a ring of `nst` stages (loaded
+//                 once when all 25 taps are resident)
+//   warps 5..     one MMA issuer (one lane) per 8-column subtile: 25 taps x
+//                 cin/16 MMAs per tile into the subtile's columns of one of
+//                 two TMEM accumulators.
+// Inputs of more than 64 channels are pipelined in units of 64 channels (a
+// halo buffer and a weight block per unit), so that two half-size halo
+// buffers overlap loads with MMAs.  Independent issuers keep several
+//                 MMA streams in flight, which the shifted (not atom-aligned)
+//                 operand windows need to reach the tensor pipe's rate.
+// Barriers (parity = use count & 1): hfull / hempty per halo buffer, afull /
+// aempty per accumulator, wfull / wempty per weight stage; the "empty" and
+// "afull" barriers count one arrival per issuer.
 // ---------------------------------------------------------------------------
 struct HaloArgs {
   int cin;               // input channels
   const bf16* wpk;       // 25 per-tap blocks of N x cin (K-major core matrices)
-  int N;                 // pad16(cout); SX * N <= 256
+  int N;                 // pad16(cout); 2 SX N <= 512
+  int nst;               // weight stages (NTAP: resident)
+  int nh;                // halo buffers (1 or 2)
   int tiles_x;           // W / (8 SX)
+  int ntiles;            // batch * (H / 16) * tiles_x
   Img g;
   Epi e;
   int* err;
 };
 
-template <int SX>
-__global__ void __launch_bounds__(128) k_conv_halo(const __grid_constant__ CUtensorMap tmap, HaloArgs a) {
+template <int SX, int KS>
+__global__ void __launch_bounds__(32 * (5 + SX)) k_conv_halo(const __grid_constant__ CUtensorMap tmap, HaloArgs a) {
   constexpr int TXH = 8 * SX + 2 * PAD;
   constexpr int SLAB = TXH * TYH * 16;     // bytes per 8 channels
+  constexpr int CH = KS > 4 ? KS / 4 : 1;  // channel units per tile
+  constexpr int KU = KS / CH;              // K steps of 16 per unit
+  constexpr int cu = 16 * KU, groups = 2 * KU;   // channels and 8-channel slabs per unit
   extern __shared__ __align__(1024) unsigned char csm[];
-  __shared__ __align__(8) uint64_t bar_h, bar_done, bar_w[NST], bar_c[NST];
+  __shared__ __align__(8) uint64_t hfull[2], hempty[2], afull[2], aempty[2], wfull[MAXST], wempty[MAXST];
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
+  __shared__ float s_bias[256];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int N = a.N, cin = a.cin, groups = cin / 8;
-  unsigned char* halo = csm;
-  unsigned char* wst = csm + (size_t)groups * SLAB;
-  const uint32_t wbytes = (uint32_t)N * cin * 2;
+  const int N = a.N, NST = a.nst, NH = a.nh;
+  const bool resident = NST >= NTAP * CH;
+  const uint32_t hbytes = (uint32_t)groups * SLAB;
+  unsigned char* halo = csm;                        // NH buffers
+  unsigned char* wst = csm + (size_t)NH * hbytes;   // NST stages
+  const uint32_t wbytes = (uint32_t)N * cu * 2;
   const int per_img = (a.g.H / TY) * a.tiles_x;
-  const int b = blockIdx.x / per_img, r = blockIdx.x - b * per_img;
-  const int y0 = (r / a.tiles_x) * TY, x0 = (r % a.tiles_x) * 8 * SX;
-  const uint32_t ncols = tmem_cols(SX * N);
+  const uint32_t acc_cols = SX * N;
+  const uint32_t ncols = tmem_cols(2 * acc_cols);
   if (warp == 0) tc::tmem_alloc(&tslot, ncols);
   if (tid == 0) {
-    tc::mbar_init(&bar_h, 1);
-    tc::mbar_init(&bar_done, 1);
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&hfull[i], 1);
+      tc::mbar_init(&hempty[i], SX);
+      tc::mbar_init(&afull[i], SX);
+      tc::mbar_init(&aempty[i], 128);
+    }
     for (int s = 0; s < NST; s++) {
-      tc::mbar_init(&bar_w[s], 1);
-      tc::mbar_init(&bar_c[s], 1);
+      tc::mbar_init(&wfull[s], 1);
+      tc::mbar_init(&wempty[s], SX);
     }
     tc::mbar_fence_init();
     s_fail = 0;
   }
+  for (int i = tid; i < N; i += blockDim.x) s_bias[i] = (a.e.bias && i < a.e.cout) ? a.e.bias[i] : 0.f;
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = tslot;
-  if (tid == 0) {
-    const uint32_t idesc = tc::idesc_bf16(TM, N);
-    tc::mbar_expect_tx(&bar_h, (uint32_t)groups * SLAB);
-    for (int gq = 0; gq < groups; gq++) tc::tma_load_4d(halo + (size_t)gq * SLAB, &tmap, 8 * gq, x0, y0, b, &bar_h);
-    for (int s = 0; s < NST; s++) {
-      tc::mbar_expect_tx(&bar_w[s], wbytes);
-      tc::bulk_load(wst + (size_t)s * wbytes, a.wpk + (size_t)s * N * cin, wbytes, &bar_w[s]);
-    }
-    bool ok = tc::mbar_wait(&bar_h, 0);
-    const uint32_t hb = tc::smem_u32(halo), wb = tc::smem_u32(wst);
-    for (int t = 0; t < NTAP && ok; t++) {
-      const int s = t % NST;
-      ok = tc::mbar_wait(&bar_w[s], (t / NST) & 1);
-      if (!ok) break;
-      tc::fence_after();
-      const int dy = t / 5, dx = t - 5 * (t / 5);
-      for (int sx = 0; sx < SX; sx++) {
-        const uint32_t a0 = hb + (uint32_t)((dy * TXH + 8 * sx + dx) * 16);
-        for (int kk = 0; kk < cin / 16; kk++) {
-          const uint64_t ad = tc::sdesc(a0 + (uint32_t)(2 * kk) * SLAB, SLAB, TXH * 16);
-          const uint64_t bd = tc::sdesc(wb + (uint32_t)s * wbytes + kk * 256, 128, cin * 16);
-          tc::mma_bf16(tmem + sx * N, ad, bd, idesc, (t | kk) ? 1u : 0u);
+  bool ok = true;
+  if (warp == 4) {
+    if (lane == 0) {
+      // producer
+      long long wq = 0;
+      int u = 0;   // pipeline unit: (tile, channel unit)
+      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+        const int b = tile / per_img, r = tile - b * per_img;
+        const int y0 = (r / a.tiles_x) * TY, x0 = (r % a.tiles_x) * 8 * SX;
+        for (int h = 0; h < CH && ok; h++, u++) {
+          const int hs = u % NH;
+          if (u >= NH) ok = tc::mbar_wait(&hempty[hs], ((u - NH) / NH) & 1);
+          if (!ok) break;
+          tc::mbar_expect_tx(&hfull[hs], hbytes);
+          for (int gq = 0; gq < groups; gq++)
+            tc::tma_load_4d(halo + (size_t)hs * hbytes + (size_t)gq * SLAB, &tmap, cu * h + 8 * gq, x0, y0, b,
+                            &hfull[hs]);
+          if (resident) {
+            if (u == 0)
+              for (int blk = 0; blk < NTAP * CH; blk++) {
+                tc::mbar_expect_tx(&wfull[blk], wbytes);
+                tc::bulk_load(wst + (size_t)blk * wbytes, a.wpk + (size_t)blk * N * cu, wbytes, &wfull[blk]);
+              }
+          } else {
+            for (int t = 0; t < NTAP && ok; t++, wq++) {
+              const int ws = (int)(wq % NST);
+              if (wq >= NST) ok = tc::mbar_wait(&wempty[ws], (int)(((wq - NST) / NST) & 1));
+              if (!ok) break;
+              tc::mbar_expect_tx(&wfull[ws], wbytes);
+              tc::bulk_load(wst + (size_t)ws * wbytes, a.wpk + (size_t)(t * CH + h) * N * cu, wbytes, &wfull[ws]);
+            }
+          }
         }
       }
-      tc::mma_commit(&bar_c[s]);
-      // refill the stage of tap t-1 (its MMAs precede tap t's in the pipe)
-      const int tp = t - 1;
-      if (tp >= 0 && tp + NST < NTAP) {
-        const int sp = tp % NST;
-        ok = tc::mbar_wait(&bar_c[sp], (tp / NST) & 1);
+    }
+    __syncwarp();
+  } else if (warp >= 5) {
+    if (lane == 0) {
+      // MMA issuer of subtile sx.  Descriptors are linear in the start
+      // address (field = address / 16): base descriptors plus offsets.
+      const int sx = warp - 5;
+      const uint32_t idesc = tc::idesc_bf16(TM, N);
+      const uint64_t ad0 = tc::sdesc(tc::smem_u32(halo), SLAB, TXH * 16) + (uint64_t)(8 * sx);
+      const uint64_t bd0 = tc::sdesc(tc::smem_u32(wst), 128, cu * 16);
+      long long wq = 0;
+      int it = 0, u = 0;
+      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x, it++) {
+        const int as = it & 1;
+        const uint32_t acc = tmem + as * acc_cols + sx * N;
+        for (int h = 0; h < CH && ok; h++, u++) {
+          const int hs = u % NH;
+          ok = tc::mbar_wait(&hfull[hs], (u / NH) & 1);
+          if (ok && h == 0 && it >= 2) ok = tc::mbar_wait(&aempty[as], ((it - 2) >> 1) & 1);
+          if (!ok) break;
+          tc::fence_after();
+          const uint64_t adh = ad0 + (uint64_t)hs * (hbytes >> 4);
+          int dy = 0, dx = 0;
+          for (int t = 0; t < NTAP && ok; t++, wq++) {
+            const int ws = resident ? t * CH + h : (int)(wq % NST);
+            // resident weights: waited for (and fenced) on the first tile only
+            if (!resident || it == 0) {
+              ok = tc::mbar_wait(&wfull[ws], resident ? 0 : (int)((wq / NST) & 1));
+              if (!ok) break;
+              tc::fence_after();
+            }
+            const uint64_t at = adh + (uint64_t)(dy * TXH + dx);
+            const uint64_t bt = bd0 + (uint64_t)ws * (wbytes >> 4);
+#pragma unroll
+            for (int kk = 0; kk < KU; kk++)
+              tc::mma_bf16(acc, at + (uint64_t)(kk * (2 * SLAB / 16)), bt + (uint64_t)(16 * kk), idesc,
+                           (t | kk | h) ? 1u : 0u);
+            if (!resident) tc::mma_commit(&wempty[ws]);
+            if (++dx == 5) { dx = 0; dy++; }
+          }
+          if (!ok) break;
+          tc::mma_commit(&hempty[hs]);
+        }
         if (!ok) break;
-        tc::mbar_expect_tx(&bar_w[sp], wbytes);
-        tc::bulk_load(wst + (size_t)sp * wbytes, a.wpk + (size_t)(tp + NST) * N * cin, wbytes, &bar_w[sp]);
+        tc::mma_commit(&afull[as]);
       }
     }
-    tc::mma_commit(&bar_done);
-    if (!ok) s_fail = 1;
+    __syncwarp();
+  } else {
+    // epilogue warps 0-3
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    int it = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, it++) {
+      const int as = it & 1;
+      const bool got = __all_sync(0xffffffffu, tc::mbar_wait(&afull[as], (it >> 1) & 1));
+      if (!got) { ok = false; break; }
+      tc::fence_after();
+      const int b = tile / per_img, r = tile - b * per_img;
+      const int y = (r / a.tiles_x) * TY + 4 * warp + (lane >> 3);
+      const int x0 = (r % a.tiles_x) * 8 * SX;
+      for (int sx = 0; sx < SX; sx++) {
+        const int x = x0 + 8 * sx + (lane & 7);
+        int n0 = 0;
+        for (; n0 + 32 <= N; n0 += 32) {
+          float v[32];
+          tc::tmem_ld32(trow + as * acc_cols + sx * N + n0, v);
+#pragma unroll
+          for (int q = 0; q < 4; q++) epilogue8(a.e, s_bias, a.g, b, y, x, n0 + 8 * q, v + 8 * q);
+        }
+        for (; n0 < N; n0 += 8) {
+          float v[8];
+          tc::tmem_ld8(trow + as * acc_cols + sx * N + n0, v);
+          epilogue8(a.e, s_bias, a.g, b, y, x, n0, v);
+        }
+      }
+      tc::fence_before();
+      tc::mbar_arrive(&aempty[as]);
+    }
   }
-  const bool done = tc::mbar_wait(&bar_done, 0);
-  const bool failed = __syncthreads_or(!done) || s_fail;
-  if (failed) {
+  if (!ok) s_fail = 1;
+  __syncthreads();
+  if (s_fail) {
     if (tid == 0) {
       atomicExch(a.err, 1);
-      // bounded waits for copies still in flight before the CTA exits
-      tc::mbar_wait(&bar_h, 0, 10000000ull);
-      for (int s = 0; s < NST; s++) tc::mbar_wait(&bar_w[s], 0, 10000000ull);
+      // give copies and MMAs still in flight a bounded time before TMEM is freed
+      tc::mbar_wait(&hfull[0], 0, 10000000ull);
+      tc::mbar_wait(&hfull[1], 0, 10000000ull);
     }
     __syncthreads();
-  } else {
-    tc::fence_after();
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    const int y = y0 + 4 * warp + (lane >> 3);
-    for (int sx = 0; sx < SX; sx++) {
-      const int x = x0 + 8 * sx + (lane & 7);
-      for (int n0 = 0; n0 < N; n0 += 8) {
-        float v[8];
-        tc::tmem_ld8(trow + sx * N + n0, v);
-        epilogue8(a.e, a.g, b, y, x, n0, v);
-      }
-    }
   }
   tc::fence_before();
   __syncthreads();
@@ -366,7 +463,7 @@ __global__ void __launch_bounds__(128) k_conv_gather(GatherArgs a) {
     for (int n0 = 0; n0 < N; n0 += 8) {
       float v[8];
       tc::tmem_ld8(trow + n0, v);
-      epilogue8(a.e, a.g, b, y, x, n0, v);
+      epilogue8(a.e, a.e.bias, a.g, b, y, x, n0, v);
     }
   }
   tc::fence_before();
@@ -380,8 +477,8 @@ __global__ void __launch_bounds__(128) k_conv_gather(GatherArgs a) {
 // image rows and adds its partial sums atomically into dw[co][tap][ci].
 // ---------------------------------------------------------------------------
 struct WgradArgs {
-  const bf16* x;   // layer input, padded NHWC (cin)
-  int cin;
+  const bf16* x;   // layer input, padded NHWC (xs channels per pixel, cin used)
+  int cin, xs;
   const bf16* g;   // gradient of the pre-activation output, padded NHWC (cout)
   int cout, N, M;  // N = pad16(cout), M = 25 cin
   Img gm;
@@ -435,7 +532,7 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
         const int tap = m / a.cin, ci0 = m - tap * a.cin;
         uint4 v = make_uint4(0, 0, 0, 0);
         if (tap < NTAP)
-          v = __ldg(reinterpret_cast<const uint4*>(a.x + a.gm.pix(b, y + tap / 5, k + tap % 5) * a.cin + ci0));
+          v = __ldg(reinterpret_cast<const uint4*>(a.x + a.gm.pix(b, y + tap / 5, k + tap % 5) * a.xs + ci0));
         const unsigned short* h = reinterpret_cast<const unsigned short*>(&v);
 #pragma unroll
         for (int j = 0; j < 8; j++)
@@ -448,7 +545,7 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
         const int tap = m / a.cin, ci = m - tap * a.cin;
         unsigned short val = 0;
         if (tap < NTAP)
-          val = __ldg(reinterpret_cast<const unsigned short*>(a.x + a.gm.pix(b, y + tap / 5, k + tap % 5) * a.cin + ci));
+          val = __ldg(reinterpret_cast<const unsigned short*>(a.x + a.gm.pix(b, y + tap / 5, k + tap % 5) * a.xs + ci));
         *reinterpret_cast<unsigned short*>(sA + tc::kmajor_off(rw, k, KC)) = val;
       }
     }
@@ -516,8 +613,9 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
 // small kernels: layout conversion, packing, loss, bias gradient, Adam
 // ---------------------------------------------------------------------------
 // NCHW (float or double) -> padded NHWC BF16 with (x - mean[c]) * inv_std[c]
+// (out has Cs >= C channels per pixel; the others are left untouched)
 template <class T>
-__global__ void k_to_nhwc(const T* __restrict__ x, bf16* __restrict__ out, int B, int C, Img g,
+__global__ void k_to_nhwc(const T* __restrict__ x, bf16* __restrict__ out, int B, int C, int Cs, Img g,
                           const float* __restrict__ mean, const float* __restrict__ inv_std) {
   const int HW = g.H * g.W;
   const size_t n = (size_t)B * C * HW;
@@ -526,7 +624,7 @@ __global__ void k_to_nhwc(const T* __restrict__ x, bf16* __restrict__ out, int B
     const size_t pix = i / C;
     const int b = (int)(pix / HW), hw = (int)(pix - (size_t)b * HW);
     const float v = (float)x[((size_t)b * C + c) * HW + hw];
-    store_px1(out, C, g, b, hw / g.W, hw % g.W, c, __float2bfloat16_rn((v - mean[c]) * inv_std[c]));
+    store_px1(out, Cs, g, b, hw / g.W, hw % g.W, c, __float2bfloat16_rn((v - mean[c]) * inv_std[c]));
   }
 }
 
@@ -551,22 +649,25 @@ __global__ void k_pack_chunks(const float* __restrict__ w, int cin, int cout, in
   }
 }
 
-// per-tap packing for the halo kernel: 25 blocks of N x kin
+// packing for the halo kernel: blocks (tap, unit) of N x cu, cu = kpad / nu
+// channels along K (kpad >= the real K channels; the padding is zero)
 __global__ void k_pack_taps(const float* __restrict__ w, int cin, int cout, int transpose, bf16* __restrict__ out,
-                            int N) {
+                            int N, int kpad, int nu) {
   const int kin = transpose ? cout : cin;
   const int nreal = transpose ? cin : cout;
-  const size_t total = (size_t)NTAP * N * kin;
+  const int cu = kpad / nu;
+  const size_t total = (size_t)NTAP * N * kpad;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-    const int tap = (int)(i / ((size_t)N * kin));
-    const int rem = (int)(i - (size_t)tap * N * kin);
-    const int n = rem / kin, ch = rem - n * kin;
+    const int blk = (int)(i / ((size_t)N * cu));
+    const int rem = (int)(i - (size_t)blk * N * cu);
+    const int n = rem / cu, cl = rem - n * cu;
+    const int tap = blk / nu, ch = (blk - tap * nu) * cu + cl;
     float v = 0.f;
-    if (n < nreal) {
+    if (n < nreal && ch < kin) {
       if (!transpose) v = w[((size_t)n * NTAP + tap) * cin + ch];
       else v = w[((size_t)ch * NTAP + (NTAP - 1 - tap)) * cin + n];
     }
-    out[(size_t)tap * N * kin + tc::kmajor_off(n, ch, kin) / 2] = __float2bfloat16_rn(v);
+    out[(size_t)blk * N * cu + tc::kmajor_off(n, cl, cu) / 2] = __float2bfloat16_rn(v);
   }
 }
 
@@ -625,6 +726,8 @@ struct ConvPlan {
   int N = 0;               // pad16(nout)
   bool halo = false;       // halo kernel (kin % 16 == 0) or gather kernel
   int sx = 0;              // halo kernel tile width / 8
+  int nst = 0;             // halo kernel weight stages
+  int nh = 0;              // halo kernel halo buffers
   int nchunk = 0;          // gather kernel K chunks
   bf16* w = nullptr;
   size_t smem = 0;
@@ -632,6 +735,7 @@ struct ConvPlan {
 
 struct CnnLayer {
   int cin, cout;
+  int cs;              // channels of the stored input activation (cin, or 16 for 1..15 inputs)
   ConvPlan fwd, bwd;
   size_t woff, boff;   // offsets into the parameter vector
 };
@@ -642,6 +746,8 @@ PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
 struct pqg_cnn {
   int nl = 0, H = 0, W = 0, maxB = 0;
+  int nsm = 1;                // SM count
+  int cps = 1;                // persistent CTAs per SM
   Img g{};
   std::vector<CnnLayer> L;
   size_t nparams = 0;
@@ -664,38 +770,44 @@ namespace {
 
 size_t gather_smem(int N) { return 2 * (size_t)CHUNK_A + 2 * (size_t)N * KC * 2; }
 
-size_t halo_smem(int sx, int kin, int N) {
-  const size_t slab = (size_t)(8 * sx + 2 * PAD) * TYH * 16;
-  return (size_t)(kin / 8) * slab + (size_t)NST * N * kin * 2;
-}
+size_t halo_bytes(int sx, int kin) { return (size_t)(kin / 8) * (8 * sx + 2 * PAD) * TYH * 16; }
 
 void plan_conv(ConvPlan& c, int W, int kin, int nout) {
   c.kin = kin;
   c.nout = nout;
   c.N = pad16(nout);
-  c.halo = kin % 16 == 0;
+  c.halo = kin == 16 || kin == 32 || kin == 64 || kin == 128;
   c.nchunk = (NTAP * kin + KC - 1) / KC;
   if (c.halo) {
-    // widest tile within 256 TMEM columns and about 110 KiB of shared memory
-    // (two CTAs per SM), else the widest that fits at all; PQG_CNN_SX caps
-    // the width (tuning)
+    // One persistent CTA per SM.  Prefer wide tiles (one MMA issuer per 8
+    // columns), then two halo buffers, then resident weights; otherwise the
+    // deepest weight ring (at least 4 stages) within about 224 KiB of shared
+    // memory.  Two accumulators of SX N columns must fit in TMEM (512).
+    // PQG_CNN_SX caps the width (tuning).
+    const size_t budget = 224 * 1024;
     int cap = 4;
     if (const char* e = getenv("PQG_CNN_SX")) cap = std::max(1, atoi(e));
-    c.sx = 0;
+    const int nu = kin > 64 ? kin / 64 : 1, cu = kin / nu;   // channel units of at most 64
+    const size_t wb = (size_t)c.N * cu * 2;
+    int best = -1;
     for (int sx : {4, 2, 1}) {
-      if (sx > cap) continue;
-      if ((W % (8 * sx)) || sx * c.N > 256) continue;
-      if (halo_smem(sx, kin, c.N) <= 110 * 1024) { c.sx = sx; break; }
+      if (sx > cap || (W % (8 * sx)) || 2 * sx * c.N > 512) continue;
+      for (int nh : {2, 1}) {
+        const size_t h = (size_t)nh * halo_bytes(sx, cu);
+        if (h >= budget) continue;
+        int nst, res;
+        if (h + (size_t)NTAP * nu * wb <= budget) { nst = NTAP * nu; res = 1; }
+        else if ((nst = (int)std::min<size_t>(NTAP * nu - 1, (budget - h) / wb)) >= 4) res = 0;
+        else continue;
+        const int score = 4 * sx + 2 * nh + res;
+        if (score > best) { best = score; c.sx = sx; c.nh = nh; c.nst = nst; }
+      }
     }
-    if (!c.sx)
-      for (int sx : {2, 1})
-        if (sx <= cap && !(W % (8 * sx)) && sx * c.N <= 256 && halo_smem(sx, kin, c.N) <= 200 * 1024) {
-          c.sx = sx;
-          break;
-        }
-    if (!c.sx) c.halo = false;
+    if (best < 0) c.halo = false;
   }
-  c.smem = c.halo ? halo_smem(c.sx, kin, c.N) : gather_smem(c.N);
+  const int nu = kin > 64 ? kin / 64 : 1;
+  c.smem = c.halo ? (size_t)c.nh * halo_bytes(c.sx, kin / nu) + (size_t)c.nst * c.N * (kin / nu) * 2
+                  : gather_smem(c.N);
 }
 
 size_t plan_weight_elems(const ConvPlan& c) {
@@ -722,6 +834,23 @@ int encode_map(CUtensorMap* m, const bf16* buf, int C, const pqg_cnn* net, int s
   return PQG_OK;
 }
 
+typedef void (*HaloFn)(const __grid_constant__ CUtensorMap, HaloArgs);
+HaloFn halo_kernel(int sx, int ks) {
+#define HK(S)                               \
+  switch (ks) {                             \
+    case 1: return k_conv_halo<S, 1>;       \
+    case 2: return k_conv_halo<S, 2>;       \
+    case 4: return k_conv_halo<S, 4>;       \
+    case 8: return k_conv_halo<S, 8>;       \
+    default: return nullptr;                \
+  }
+  if (sx == 4) { HK(4) }
+  if (sx == 2) { HK(2) }
+  if (sx == 1) { HK(1) }
+#undef HK
+  return nullptr;
+}
+
 int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int batch, const Epi& e,
                 cudaStream_t st) {
   const ConvPlan& c = dgrad ? l.bwd : l.fwd;
@@ -733,16 +862,17 @@ int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int
     a.cin = c.kin;
     a.wpk = c.w;
     a.N = c.N;
+    a.nst = c.nst;
+    a.nh = c.nh;
     a.tiles_x = net->W / (8 * c.sx);
+    a.ntiles = batch * (net->H / TY) * a.tiles_x;
     a.g = net->g;
     a.e = e;
     a.err = net->err;
-    const dim3 grid(batch * (net->H / TY) * a.tiles_x);
-    switch (c.sx) {
-      case 4: k_conv_halo<4><<<grid, TM, c.smem, st>>>(m, a); break;
-      case 2: k_conv_halo<2><<<grid, TM, c.smem, st>>>(m, a); break;
-      default: k_conv_halo<1><<<grid, TM, c.smem, st>>>(m, a); break;
-    }
+    const dim3 grid(std::min(a.ntiles, net->nsm * net->cps));
+    auto fn = halo_kernel(c.sx, c.kin / 16);
+    if (!fn) return cfail(PQG_ERR_UNSUPPORTED, "no convolution kernel for this channel count");
+    fn<<<grid, 32 * (5 + c.sx), c.smem, st>>>(m, a);
   } else {
     GatherArgs a;
     a.in = in;
@@ -764,6 +894,7 @@ int launch_wgrad(pqg_cnn* net, const CnnLayer& l, const bf16* x, const bf16* g, 
   WgradArgs a;
   a.x = x;
   a.cin = l.cin;
+  a.xs = l.cs;
   a.g = g;
   a.cout = l.cout;
   a.N = pad16(l.cout);
@@ -797,9 +928,9 @@ int set_attrs() {
   CCUDA(cudaGetDevice(&dev));
   CCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const int big = optin - 2048;
-  CCUDA(cudaFuncSetAttribute(k_conv_halo<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  CCUDA(cudaFuncSetAttribute(k_conv_halo<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  CCUDA(cudaFuncSetAttribute(k_conv_halo<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  for (int sx : {1, 2, 4})
+    for (int ks : {1, 2, 4, 8})
+      CCUDA(cudaFuncSetAttribute(halo_kernel(sx, ks), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_conv_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_wgrad<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_wgrad<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -815,7 +946,8 @@ int repack(pqg_cnn* net, cudaStream_t st) {
     for (int d = 0; d < 2; d++) {
       const ConvPlan& c = d ? l.bwd : l.fwd;
       if (c.halo)
-        k_pack_taps<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w, c.N);
+        k_pack_taps<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w, c.N,
+                                                                   c.kin, c.kin > 64 ? c.kin / 64 : 1);
       else
         k_pack_chunks<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w,
                                                                      c.N, c.nchunk);
@@ -881,12 +1013,22 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
   net->W = width;
   net->maxB = max_batch;
   net->g = Img{height, width, height + 2 * PAD, width + 2 * PAD};
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&net->nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (net->nsm < 1) net->nsm = 1;
+    if (const char* e = getenv("PQG_CNN_CPS")) net->cps = std::max(1, std::min(4, atoi(e)));
+  }
   size_t off = 0;
   for (int i = 0; i < nlayers; i++) {
     CnnLayer l{};
     l.cin = channels[i];
     l.cout = channels[i + 1];
-    plan_conv(l.fwd, width, l.cin, l.cout);
+    // the network input (few channels) is stored zero-padded to 16 channels
+    // so that the first layer runs on the halo kernel
+    l.cs = (i == 0 && l.cin < 16) ? 16 : l.cin;
+    plan_conv(l.fwd, width, l.cs, l.cout);
     plan_conv(l.bwd, width, l.cout, l.cin);
     l.woff = off;
     off += (size_t)l.cout * NTAP * l.cin;
@@ -914,7 +1056,8 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
   }
   net->act.assign(nlayers, nullptr);
   for (int i = 0; i < nlayers; i++)
-    if (cudaMalloc(&net->act[i], npad * net->L[i].cin * 2)) return fail("activations");
+    if (cudaMalloc(&net->act[i], npad * net->L[i].cs * 2) || cudaMemset(net->act[i], 0, npad * net->L[i].cs * 2))
+      return fail("activations");
   if (cudaMalloc(&net->out, npix * net->L.back().cout * 4) || cudaMalloc(&net->ga, npad * net->cmax * 2) ||
       cudaMalloc(&net->gb, npad * net->cmax * 2) || cudaMalloc(&net->norm, 4 * 6 * 128) ||
       cudaMalloc(&net->loss, 4) || cudaMalloc(&net->err, 4))
@@ -1036,11 +1179,11 @@ PQG_API int pqg_cnn_forward(pqg_cnn* net, const void* x, int x_f64, void* y, int
   cudaStream_t st = (cudaStream_t)stream;
   const size_t n = (size_t)batch * net->L[0].cin * net->H * net->W;
   if (x_f64)
-    k_to_nhwc<double><<<grid_for(n), 256, 0, st>>>((const double*)x, net->act[0], batch, net->L[0].cin, net->g,
-                                                   net->norm, net->norm + 128);
+    k_to_nhwc<double><<<grid_for(n), 256, 0, st>>>((const double*)x, net->act[0], batch, net->L[0].cin,
+                                                   net->L[0].cs, net->g, net->norm, net->norm + 128);
   else
-    k_to_nhwc<float><<<grid_for(n), 256, 0, st>>>((const float*)x, net->act[0], batch, net->L[0].cin, net->g,
-                                                  net->norm, net->norm + 128);
+    k_to_nhwc<float><<<grid_for(n), 256, 0, st>>>((const float*)x, net->act[0], batch, net->L[0].cin, net->L[0].cs,
+                                                  net->g, net->norm, net->norm + 128);
   CCUDA(cudaGetLastError());
   return forward_layers(net, batch, y, y_f64, net->norm + 256, net->norm + 384, st);
 }
@@ -1054,8 +1197,8 @@ PQG_API int pqg_cnn_backward(pqg_cnn* net, const float* x, const float* t, int b
   const size_t npix = (size_t)batch * net->H * net->W;
   const float* ones = net->norm + 512;
   const float* zeros = net->norm + 640;
-  k_to_nhwc<float><<<grid_for(npix * net->L[0].cin), 256, 0, st>>>(x, net->act[0], batch, net->L[0].cin, net->g,
-                                                                   zeros, ones);
+  k_to_nhwc<float><<<grid_for(npix * net->L[0].cin), 256, 0, st>>>(x, net->act[0], batch, net->L[0].cin,
+                                                                   net->L[0].cs, net->g, zeros, ones);
   CCUDA(cudaGetLastError());
   int rc = forward_layers(net, batch, net->out, 0, ones, zeros, st);
   if (rc) return rc;
