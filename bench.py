@@ -378,7 +378,77 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks.summary(),
         "gpu_launches": args.steps * (2 * args.chunk + 2),
     }
+    if world == 1 and not args.no_closure:
+        try:
+            line["closure"] = closure_throughput(args, value)
+        except Exception as exc:      # reported, the main line stands
+            line["closure"] = {"error": "%s: %s" % (type(exc).__name__, exc)}
     print(json.dumps(line), flush=True)
+
+
+def closure_throughput(args, plain_value):
+    """Config-5 workload: two-layer nx=64 FP32 members with the 8-layer
+    convolutional closure applied every step (and the same ensemble without
+    it), aggregate simulated years per wall-clock hour over the members.
+    The network is randomly initialised: its cost does not depend on the
+    weights."""
+    import torch
+    import pyqg_gb300 as P
+    from pyqg_gb300.closure import CNNParameterization, ConvNet
+    from pyqg_gb300.coarsen import PHYSICS
+    B, dt, chunk = args.closure_members, 7200.0, args.closure_chunk
+    members = [("qg", dict(nx=64, dt=dt, **PHYSICS))] * B
+    rng = np.random.default_rng(3000)
+    qs = [1e-7 * rng.standard_normal((2, 64, 64)) for _ in range(B)]
+    net = ConvNet(max_batch=B, seed=0)
+    CNNParameterization(net, ([0.0, 0.0], [1e-6, 1e-7], [0.0, 0.0], [1e-12, 1e-13]))
+    stream = torch.cuda.current_stream()
+    res = {"workload": "%d two-layer QG members nx=64 dt=7200 FP32 (FP64-built matrices), "
+                       "8-layer 5x5 CNN closure (2-128-64-32-32-32-32-32-2, BF16 tcgen05) every step; "
+                       "%d steps per timed step" % (B, chunk)}
+    for name, closure in (("closure", True), ("no_closure", False)):
+        ens = P.Ensemble(members, precision="fp32")
+        ens.set_q(qs)
+        if closure:
+            ens.set_closure(net)
+        for _ in range(max(1, args.warmup)):
+            ens.step(chunk)
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.closure_steps)]
+        for a, b in evs:
+            a.record(stream)
+            ens.step(chunk)
+            b.record(stream)
+        torch.cuda.synchronize()
+        sec = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        res[name] = {"value": sim_yr_per_hr(B * chunk * args.closure_steps, dt, sec),
+                     "ms_per_model_step": 1e3 * sec / (chunk * args.closure_steps)}
+        del ens
+    x = torch.randn(B, 2, 64, 64, device="cuda")
+    y = torch.empty_like(x)
+    for _ in range(3):
+        net.forward(x, y)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(10):
+        net.forward(x, y)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    cnn_ms = e0.elapsed_time(e1) / 10
+    flops = 2.0 * 366400 * B * 64 * 64
+    bf16 = None
+    pk = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as f:
+            bf16 = json.load(f).get("bf16_tflops")
+    tfs = flops / (cnn_ms * 1e-3) / 1e12
+    res["cnn_forward"] = {"ms": cnn_ms, "tflops": tfs, "peak_tflops": bf16,
+                          "frac": (tfs / bf16) if bf16 else None, "unit": "TFLOP/s",
+                          "bound": "tensor", "peak_source": "measured" if bf16 else None}
+    res["unit"] = "sim-yr/hr (sum over members)"
+    res["vs_nx256_plain_fp64"] = res["closure"]["value"] / plain_value if plain_value else None
+    return res
 
 
 def main():
@@ -390,6 +460,10 @@ def main():
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--cpu-sample", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--closure-members", type=int, default=512)
+    ap.add_argument("--closure-steps", type=int, default=5)
+    ap.add_argument("--closure-chunk", type=int, default=100)
+    ap.add_argument("--no-closure", action="store_true", help="skip the closure-ensemble measurement")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

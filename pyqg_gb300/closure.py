@@ -35,8 +35,9 @@ class ConvNet:
     """Fully convolutional net with 5x5 periodic kernels.
 
     ``channels`` lists the channel counts from input to output; images are
-    ``(batch, channels, ny, 64)``.  Parameters are initialised He-uniform
-    (weights) and zero (biases) from ``seed``.
+    ``(batch, channels, ny, 64)``.  Weights and biases are initialised
+    uniform in +-1/sqrt(fan_in) from ``seed`` (the usual default for
+    convolutions, which Adam at lr 1e-3 expects).
     """
 
     def __init__(self, channels=DEFAULT_CHANNELS, ny=64, nx=64, max_batch=64, seed=0):
@@ -70,8 +71,9 @@ class ConvNet:
         p = np.zeros(self.nparams, dtype=np.float32)
         for ws, shape, bs in self.layer_slices():
             fan_in = shape[1] * shape[2] * shape[3]
-            bound = np.sqrt(6.0 / fan_in)
+            bound = 1.0 / np.sqrt(fan_in)
             p[ws] = rng.uniform(-bound, bound, size=ws.stop - ws.start).astype(np.float32)
+            p[bs] = rng.uniform(-bound, bound, size=bs.stop - bs.start).astype(np.float32)
         return p
 
     def _check(self, rc):

@@ -55,12 +55,13 @@ class CoarseGrainer:
 
 def generate_training_data(nruns=64, nx_fine=256, nx_coarse=64, dt=3600.0, spinup_steps=86400,
                            snapshot_interval=1000, nsnapshots=780, seed0=2000, physics=None,
-                           progress=None):
+                           progress=None, return_ensemble=False):
     """(X, Y) CUDA float32 tensors (N, 2, nx_coarse, nx_coarse) of coarse PV
     and subgrid forcing from `nruns` FP64 fine runs (initial PV 1e-7 N(0, 1)
     seeded by seed0 + i), snapshots every `snapshot_interval` steps after
     `spinup_steps`.  Defaults: 64 runs, 10 years of spin-up (360-day years)
-    and snapshots every 1000 h."""
+    and snapshots every 1000 h.  With `return_ensemble` the fine ensemble
+    (at the last snapshot) is returned too."""
     import torch
     from .ensemble import Ensemble
     from .qg_model import QGModel
@@ -90,6 +91,8 @@ def generate_training_data(nruns=64, nx_fine=256, nx_coarse=64, dt=3600.0, spinu
             Y[s * nruns + i] = S
         if progress:
             progress(s, nsnapshots)
+    if return_ensemble:
+        return X, Y, ens
     return X, Y
 
 

@@ -200,3 +200,61 @@ def test_ensemble_closure_fp32_runs():
     ens.step(20)
     torch.cuda.synchronize()
     assert all(np.all(np.isfinite(ens.q(i))) for i in range(8))
+
+
+@pytest.mark.parametrize("batch", [48, 160])
+def test_forward_many_tiles_per_cta(batch):
+    """Batches large enough that every persistent CTA processes several tiles
+    (buffer and accumulator reuse across tiles)."""
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    channels = (2, 128, 64, 32, 32, 32, 32, 32, 2)
+    net = ConvNet(channels, max_batch=batch, seed=5)
+    p = net.params
+    rng = np.random.default_rng(4)
+    p += (0.05 * rng.standard_normal(p.shape)).astype(np.float32)
+    net.params = p
+    x = torch.from_numpy(rng.standard_normal((batch, 2, 64, 64)).astype(np.float32)).cuda()
+    y = net.forward(x)
+    torch.cuda.synchronize()
+    ref = _torch_net(channels, p, net.layer_slices(), x)
+    err = rel_l2(y.cpu().numpy(), ref.cpu().numpy())
+    assert err < 1e-2, err
+    # every image separately: no tile of any image may be wrong
+    for b in range(batch):
+        assert rel_l2(y[b].cpu().numpy(), ref[b].cpu().numpy()) < 2e-2, b
+
+
+def test_gradients_many_tiles_per_cta():
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    channels = (2, 128, 64, 32, 32, 32, 32, 32, 2)
+    batch = 48
+    net = ConvNet(channels, max_batch=batch, seed=8)
+    p = net.params
+    rng = np.random.default_rng(6)
+    p += (0.02 * rng.standard_normal(p.shape)).astype(np.float32)
+    net.params = p
+    x = torch.from_numpy(rng.standard_normal((batch, 2, 64, 64)).astype(np.float32)).cuda()
+    t = torch.from_numpy(rng.standard_normal((batch, 2, 64, 64)).astype(np.float32)).cuda()
+    loss = net.backward(x, t)
+    g = net.grads
+    ref_loss, ref = _reference_grads(channels, p, net.layer_slices(), x, t)
+    assert abs(loss - ref_loss) / ref_loss < 1e-2
+    for (ws, shape, bs), (gw, gb) in zip(net.layer_slices(), ref):
+        assert rel_l2(g[ws].reshape(shape), gw) < 5e-2
+        assert rel_l2(g[bs], gb) < 5e-2
+
+
+def test_default_net_learns():
+    """The 8-layer network fits a fixed local linear map of its input."""
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    net = ConvNet(max_batch=32, seed=9)
+    rng = np.random.default_rng(7)
+    x = torch.from_numpy(rng.standard_normal((32, 2, 64, 64)).astype(np.float32)).cuda()
+    lap = (torch.roll(x, 1, 2) + torch.roll(x, -1, 2) + torch.roll(x, 1, 3) + torch.roll(x, -1, 3) - 4 * x)
+    t = (lap / lap.std()).contiguous()
+    losses = [net.train_step(x, t, lr=1e-3) for _ in range(150)]
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.3 * losses[0], (losses[0], losses[-1])
