@@ -248,6 +248,42 @@ int pqg_coarse_forcing(pqg_plan *fine, pqg_plan *coarse, const double *qh_f,
                        double *q_c, double *S, void *stream);
 
 /* ---------------------------------------------------------------------
+ * Diagnostics on the device (replaces the host accumulation loop,
+ * pyqg/model.py:802-814): pqg_diag_accumulate adds one step's value of a
+ * built-in diagnostic to a device FP64 accumulator (acc += value), with the
+ * formulas of pyqg/model.py:640-760, pyqg/qg_diagnostics.py,
+ * pyqg/qg_model.py:231-263 and pyqg/layered_model.py:261-300.
+ * Accumulator shapes: (nz, nl, nk) for ENSSPEC, KESPEC, KESPEC_MODAL;
+ * (nz-1, nl, nk) for PESPEC_MODAL; (nz) for EKE; scalar for EKEDISS and
+ * APEGEN; (nl, nk) otherwise.  Spectral fields are complex (re, im) device
+ * arrays of (nz, nl, nk) (Jptpc: one plane); u, v are physical (nz, ny, nx).
+ * Unused fields may be NULL; a missing required field is PQG_ERR_INVALID.
+ * --------------------------------------------------------------------- */
+#define PQG_DIAG_MAXZ 8
+enum {
+  PQG_DIAG_ENSSPEC = 0, PQG_DIAG_KESPEC, PQG_DIAG_EKE, PQG_DIAG_EKEDISS,
+  PQG_DIAG_KEFRICTIONSPEC, PQG_DIAG_DISSSPEC, PQG_DIAG_ENSDISSSPEC,
+  PQG_DIAG_PARAMSPEC, PQG_DIAG_ENSPARAMSPEC, PQG_DIAG_ENTSPEC,
+  PQG_DIAG_PARAMSPEC_APEFLUX, PQG_DIAG_PARAMSPEC_KEFLUX, PQG_DIAG_ENSFLUX,
+  PQG_DIAG_ENSGENSPEC, PQG_DIAG_ENSFRICTIONSPEC, PQG_DIAG_APEGENSPEC,
+  PQG_DIAG_APEFLUX, PQG_DIAG_KEFLUX, PQG_DIAG_APEGEN, PQG_DIAG_KESPEC_MODAL,
+  PQG_DIAG_PESPEC_MODAL, PQG_DIAG_APESPEC, PQG_DIAG_KEFLUX_DIV,
+  PQG_DIAG_APEFLUX_DIV, PQG_DIAG_COUNT
+};
+typedef struct pqg_diag_fields {
+  const double *qh, *ph, *dqhdt, *dqhdt_p, *dqhdt_pp; /* spectral state  */
+  const double *u, *v;                                /* physical        */
+  const double *Jq, *Jpxi, *Jptpc, *JSp, *Sph, *phn;  /* derived fields  */
+  const double *dqh, *duh, *dvh;                      /* hook outputs    */
+  /* host scalars / per-layer arrays */
+  double H, dt, c1, c2, c3;        /* depth, dt, AB coefficients of the step */
+  double rd, del1, del2, U;        /* two-layer constants                    */
+  const double *Hi, *Qx, *Qy, *Ubg, *Vbg, *f2gpi, *kdi2, *S; /* S: nz x nz  */
+} pqg_diag_fields;
+int pqg_diag_accumulate(pqg_plan *plan, int kind, const pqg_diag_fields *f,
+                        double *acc, void *stream);
+
+/* ---------------------------------------------------------------------
  * Learned subgrid closure (no counterpart in the reference): a fully
  * convolutional network of 5x5 periodic convolutions with ReLU between
  * layers, BF16 weights and activations, FP32 accumulation on the tcgen05

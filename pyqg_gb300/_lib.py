@@ -34,6 +34,17 @@ class State(ctypes.Structure):
                 ("t", _D), ("dt", _D)]
 
 
+_PD = ctypes.POINTER(ctypes.c_double)
+
+
+class DiagFields(ctypes.Structure):
+    """pqg_diag_fields (include/pyqg_gb300.h)."""
+    _fields_ = ([(n, _PD) for n in ("qh", "ph", "dqhdt", "dqhdt_p", "dqhdt_pp", "u", "v", "Jq",
+                                    "Jpxi", "Jptpc", "JSp", "Sph", "phn", "dqh", "duh", "dvh")] +
+                [(n, _D) for n in ("H", "dt", "c1", "c2", "c3", "rd", "del1", "del2", "U")] +
+                [(n, _PD) for n in ("Hi", "Qx", "Qy", "Ubg", "Vbg", "f2gpi", "kdi2", "S")])
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "pqg_version": (_I, []),
@@ -76,6 +87,7 @@ SIGNATURES = {
     "pqg_ens_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
                            ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_D)]),
     "pqg_advect": (_I, [_P, _P, _P, _P, _I, _P, _P]),
+    "pqg_diag_accumulate": (_I, [_P, _I, ctypes.POINTER(DiagFields), _P, _P]),
     "pqg_coarse_forcing": (_I, [_P, _P, _P, _P, _P, _P]),
     "pqg_cnn_last_error": (ctypes.c_char_p, []),
     "pqg_cnn_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _I, _I]),

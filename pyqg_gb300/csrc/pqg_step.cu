@@ -1964,4 +1964,316 @@ PQG_API int pqg_coarse_forcing(pqg_plan* pf, pqg_plan* pc, const double* qh_f, d
   return pqg_irfft2(pc, reinterpret_cast<const double*>(qbar), S, nz, st);
 }
 
+// ---------------------------------------------------------------------------
+// diagnostics: FP64 accumulation on the device of the models' built-in
+// diagnostics (pyqg/model.py:640-760, pyqg/qg_diagnostics.py:1-75,
+// pyqg/qg_model.py:213-263, pyqg/layered_model.py:242-300), replacing the
+// host loop of pyqg/model.py:802-814.  One thread per (l, k) for the
+// spectral diagnostics (deterministic), block reductions with FP64 atomics
+// for the domain totals.
+// ---------------------------------------------------------------------------
+struct DiagParams {
+  int kind, nz, ny, nk, nx;
+  double M2, H, rek, dt, c1, c2, c3, rd, del1, del2, U;
+  double Hi[PQG_DIAG_MAXZ], Qx[PQG_DIAG_MAXZ], Qy[PQG_DIAG_MAXZ], Ubg[PQG_DIAG_MAXZ], Vbg[PQG_DIAG_MAXZ];
+  double f2gpi[PQG_DIAG_MAXZ], kdi2[PQG_DIAG_MAXZ], S[PQG_DIAG_MAXZ * PQG_DIAG_MAXZ];
+};
+
+__device__ __forceinline__ double2 cget(const double* p, size_t i) {
+  return reinterpret_cast<const double2*>(p)[i];
+}
+__device__ __forceinline__ double re_conj_mul(double2 a, double2 b) {   // Re(conj(a) b)
+  return a.x * b.x + a.y * b.y;
+}
+__device__ __forceinline__ double abs2(double2 a) { return a.x * a.x + a.y * a.y; }
+
+// parameterization contribution dqh + (-il duh + ik dvh) of layer z at i
+__device__ __forceinline__ double2 param_contrib(const pqg_diag_fields& f, size_t o, double kx, double ly) {
+  double2 r = make_double2(0.0, 0.0);
+  if (f.duh && f.dvh) {
+    const double2 du = cget(f.duh, o), dv = cget(f.dvh, o);
+    // -il duh + ik dvh = (ly du.y - kx dv.y) + i(-ly du.x + kx dv.x)
+    r.x += ly * du.y - kx * dv.y;
+    r.y += -ly * du.x + kx * dv.x;
+  }
+  if (f.dqh) {
+    const double2 d = cget(f.dqh, o);
+    r.x += d.x;
+    r.y += d.y;
+  }
+  return r;
+}
+
+__global__ void k_diag_spec(DiagParams P, pqg_diag_fields f, const double* __restrict__ a,
+                            const double* __restrict__ kk, const double* __restrict__ ll,
+                            const double* __restrict__ k2l2, const double* __restrict__ filtr, double* acc) {
+  const int nz = P.nz, n = P.ny * P.nk;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int k = i % P.nk, l = i / P.nk;
+    const double kx = kk[k], ly = ll[l], wv2 = k2l2[i];
+    auto at = [&](int z) { return (size_t)z * n + i; };
+    switch (P.kind) {
+      case PQG_DIAG_ENSSPEC:
+        for (int z = 0; z < nz; z++) acc[at(z)] += abs2(cget(f.qh, at(z))) / P.M2;
+        break;
+      case PQG_DIAG_KESPEC:
+        for (int z = 0; z < nz; z++) acc[at(z)] += wv2 * abs2(cget(f.ph, at(z))) / P.M2;
+        break;
+      case PQG_DIAG_KEFRICTIONSPEC:
+        acc[i] += -P.rek * P.Hi[nz - 1] / P.H * wv2 * abs2(cget(f.ph, at(nz - 1))) / P.M2;
+        break;
+      case PQG_DIAG_DISSSPEC:
+      case PQG_DIAG_ENSDISSSPEC: {
+        double s = 0.0;
+        const double fm1 = filtr[i] - 1.0;
+        for (int z = 0; z < nz; z++) {
+          const double2 q = cget(f.qh, at(z)), d = cget(f.dqhdt, at(z)), dp = cget(f.dqhdt_p, at(z)),
+                        dpp = cget(f.dqhdt_pp, at(z));
+          double2 fd;
+          fd.x = fm1 * (((q.x + P.c1 * d.x) + P.c2 * dp.x) + P.c3 * dpp.x);
+          fd.y = fm1 * (((q.y + P.c1 * d.y) + P.c2 * dp.y) + P.c3 * dpp.y);
+          const double2 w = P.kind == PQG_DIAG_DISSSPEC ? cget(f.ph, at(z)) : q;
+          s += P.Hi[z] * re_conj_mul(w, fd);
+        }
+        acc[i] += (P.kind == PQG_DIAG_DISSSPEC ? -s : s) / P.H / P.dt / P.M2;
+        break;
+      }
+      case PQG_DIAG_ENTSPEC: {
+        double2 t = make_double2(0.0, 0.0);
+        for (int z = 0; z < nz; z++) {
+          const double2 q = cget(f.qh, at(z));
+          t.x += P.Hi[z] * q.x;
+          t.y += P.Hi[z] * q.y;
+        }
+        t.x /= P.H;
+        t.y /= P.H;
+        acc[i] += abs2(t) / P.M2;
+        break;
+      }
+      case PQG_DIAG_ENSFLUX:
+      case PQG_DIAG_KEFLUX_DIV:
+      case PQG_DIAG_APEFLUX_DIV: {
+        const double* J = P.kind == PQG_DIAG_ENSFLUX ? f.Jq : (P.kind == PQG_DIAG_KEFLUX_DIV ? f.Jpxi : f.JSp);
+        const double* X = P.kind == PQG_DIAG_ENSFLUX ? f.qh : f.ph;
+        double s = 0.0;
+        for (int z = 0; z < nz; z++) s += P.Hi[z] * re_conj_mul(cget(X, at(z)), cget(J, at(z)));
+        s = s / P.H / P.M2;
+        acc[i] += P.kind == PQG_DIAG_ENSFLUX ? -s : s;
+        break;
+      }
+      case PQG_DIAG_ENSFRICTIONSPEC:
+        acc[i] += P.rek * P.Hi[nz - 1] / P.H * wv2 * re_conj_mul(cget(f.qh, at(nz - 1)), cget(f.ph, at(nz - 1))) / P.M2;
+        break;
+      case PQG_DIAG_ENSGENSPEC: {
+        double s = 0.0;
+        for (int z = 0; z < nz; z++) {
+          // Re(i c conj(Sph) ph), c = l Qx - k Qy
+          const double c = ly * P.Qx[z] - kx * P.Qy[z];
+          const double2 sp = cget(f.Sph, at(z)), p = cget(f.ph, at(z));
+          const double im = sp.x * p.y - sp.y * p.x;   // Im(conj(Sph) ph)
+          s += P.Hi[z] * (-c * im);
+        }
+        acc[i] += s / P.H / P.M2;
+        break;
+      }
+      case PQG_DIAG_APEGENSPEC: {
+        double s = 0.0;
+        for (int z = 0; z < nz; z++) {
+          // Re((U k + V l) i conj(ph) Sph)
+          const double c = P.Ubg[z] * kx + P.Vbg[z] * ly;
+          const double2 p = cget(f.ph, at(z)), sp = cget(f.Sph, at(z));
+          const double im = p.x * sp.y - p.y * sp.x;   // Im(conj(ph) Sph)
+          s += P.Hi[z] * (-c * im);
+        }
+        acc[i] += s / P.H / P.M2;
+        break;
+      }
+      case PQG_DIAG_KEFLUX: {
+        const double2 p0 = cget(f.ph, at(0)), p1 = cget(f.ph, at(1));
+        const double2 j0 = cget(f.Jpxi, at(0)), j1 = cget(f.Jpxi, at(1));
+        acc[i] += (P.del1 * re_conj_mul(j0, p0) + P.del2 * re_conj_mul(j1, p1)) / P.M2;
+        break;
+      }
+      case PQG_DIAG_APEFLUX: {
+        const double2 p0 = cget(f.ph, at(0)), p1 = cget(f.ph, at(1));
+        const double2 d = make_double2(p0.x - p1.x, p0.y - p1.y);
+        acc[i] += 1.0 / (P.rd * P.rd) * P.del1 * P.del2 * re_conj_mul(cget(f.Jptpc, i), d) / P.M2;
+        break;
+      }
+      case PQG_DIAG_APESPEC: {
+        double s = 0.0;
+        for (int z = 0; z + 1 < nz; z++) {
+          const double2 p0 = cget(f.ph, at(z)), p1 = cget(f.ph, at(z + 1));
+          s += P.f2gpi[z] * abs2(make_double2(p0.x - p1.x, p0.y - p1.y));
+        }
+        acc[i] += s / P.H / P.M2;
+        break;
+      }
+      case PQG_DIAG_KESPEC_MODAL:
+        for (int z = 0; z < nz; z++) acc[at(z)] += wv2 * abs2(cget(f.phn, at(z))) / P.M2;
+        break;
+      case PQG_DIAG_PESPEC_MODAL:
+        for (int z = 1; z < nz; z++) acc[at(z - 1)] += P.kdi2[z] * abs2(cget(f.phn, at(z))) / P.M2;
+        break;
+      case PQG_DIAG_PARAMSPEC:
+      case PQG_DIAG_ENSPARAMSPEC: {
+        double s = 0.0;
+        for (int z = 0; z < nz; z++) {
+          const double2 dq = param_contrib(f, at(z), kx, ly);
+          const double2 w = P.kind == PQG_DIAG_PARAMSPEC ? cget(f.ph, at(z)) : cget(f.qh, at(z));
+          s += P.Hi[z] / P.H * re_conj_mul(w, dq);
+        }
+        acc[i] += (P.kind == PQG_DIAG_PARAMSPEC ? -s : s) / P.M2;
+        break;
+      }
+      case PQG_DIAG_PARAMSPEC_KEFLUX:
+      case PQG_DIAG_PARAMSPEC_APEFLUX: {
+        double2 dq[PQG_DIAG_MAXZ], adq[PQG_DIAG_MAXZ];
+        for (int z = 0; z < nz; z++) dq[z] = param_contrib(f, at(z), kx, ly);
+        for (int z = 0; z < nz; z++) {
+          double2 t = make_double2(0.0, 0.0);
+          for (int z1 = 0; z1 < nz; z1++) {
+            const double c = a[(size_t)(z * nz + z1) * n + i];
+            t.x += c * dq[z1].x;
+            t.y += c * dq[z1].y;
+          }
+          adq[z] = t;
+        }
+        double s = 0.0;
+        for (int z = 0; z < nz; z++) {
+          double2 term = adq[z];
+          if (P.kind == PQG_DIAG_PARAMSPEC_APEFLUX) {
+            term = make_double2(0.0, 0.0);
+            for (int z1 = 0; z1 < nz; z1++) {
+              term.x += P.S[z * nz + z1] * adq[z1].x;
+              term.y += P.S[z * nz + z1] * adq[z1].y;
+            }
+          }
+          s += P.Hi[z] / P.H * re_conj_mul(cget(f.ph, at(z)), term);
+        }
+        s /= P.M2;
+        acc[i] += P.kind == PQG_DIAG_PARAMSPEC_KEFLUX ? wv2 * s : -s;
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
+// domain totals: EKE (per layer), EKEdiss, APEgen
+__global__ void k_diag_sum(DiagParams P, pqg_diag_fields f, const double* __restrict__ kk, double* acc) {
+  const int nz = P.nz;
+  const size_t plane = (size_t)P.ny * P.nx;
+  __shared__ double red[32];
+  const int nout = P.kind == PQG_DIAG_EKE ? nz : 1;
+  for (int o = 0; o < nout; o++) {
+    double s = 0.0;
+    if (P.kind == PQG_DIAG_EKE || P.kind == PQG_DIAG_EKEDISS) {
+      const int z = P.kind == PQG_DIAG_EKE ? o : nz - 1;
+      for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < plane; i += (size_t)gridDim.x * blockDim.x) {
+        const double u = f.u[(size_t)z * plane + i], v = f.v[(size_t)z * plane + i];
+        s += v * v + u * u;
+      }
+    } else {   // APEgen: -k Im(bt conj(bc)), interior columns 1..nk-3 counted twice
+      const size_t n = (size_t)P.ny * P.nk;
+      for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(i % P.nk);
+        const double2 p0 = cget(f.ph, i), p1 = cget(f.ph, n + i);
+        const double2 bt = make_double2(P.del1 * p0.x + P.del2 * p1.x, P.del1 * p0.y + P.del2 * p1.y);
+        const double2 bc = make_double2(p0.x - p1.x, p0.y - p1.y);
+        const double im = bt.y * bc.x - bt.x * bc.y;   // Im(bt conj(bc))
+        const double v = -kk[k] * im;
+        s += (k >= 1 && k <= P.nk - 3) ? 2.0 * v : v;
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[w] = s;
+    __syncthreads();
+    if (w == 0) {
+      s = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) {
+        double scale;
+        if (P.kind == PQG_DIAG_EKE) scale = 0.5 / (double)plane;
+        else if (P.kind == PQG_DIAG_EKEDISS) scale = P.Hi[nz - 1] / P.H * P.rek / (double)plane;
+        else scale = P.U / (P.rd * P.rd) * P.del1 * P.del2 / P.M2;
+        atomicAdd(acc + o, s * scale);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+PQG_API int pqg_diag_accumulate(pqg_plan* p, int kind, const pqg_diag_fields* f, double* acc, void* stream) {
+  if (!p || !f || !acc) return fail(PQG_ERR_INVALID, "NULL argument to pqg_diag_accumulate");
+  if (p->nz > PQG_DIAG_MAXZ) return fail(PQG_ERR_UNSUPPORTED, "too many layers for the device diagnostics");
+  if (!p->have_kk || !p->have_ll) return fail(PQG_ERR_STATE, "wavenumbers not set");
+  if (kind < 0 || kind >= PQG_DIAG_COUNT) return fail(PQG_ERR_INVALID, "unknown diagnostic");
+  DiagParams P{};
+  P.kind = kind;
+  P.nz = p->nz;
+  P.ny = p->ny;
+  P.nk = p->nk;
+  P.nx = p->nx;
+  P.M2 = (double)p->nx * p->ny * (double)p->nx * p->ny;
+  P.H = f->H;
+  P.rek = p->rek;
+  P.dt = f->dt;
+  P.c1 = f->c1;
+  P.c2 = f->c2;
+  P.c3 = f->c3;
+  P.rd = f->rd;
+  P.del1 = f->del1;
+  P.del2 = f->del2;
+  P.U = f->U;
+  for (int z = 0; z < p->nz; z++) {
+    P.Hi[z] = f->Hi ? f->Hi[z] : 0.0;
+    P.Qx[z] = f->Qx ? f->Qx[z] : 0.0;
+    P.Qy[z] = f->Qy ? f->Qy[z] : 0.0;
+    P.Ubg[z] = f->Ubg ? f->Ubg[z] : 0.0;
+    P.Vbg[z] = f->Vbg ? f->Vbg[z] : 0.0;
+    P.f2gpi[z] = f->f2gpi ? f->f2gpi[z] : 0.0;
+    P.kdi2[z] = f->kdi2 ? f->kdi2[z] : 0.0;
+    for (int z1 = 0; z1 < p->nz; z1++) P.S[z * p->nz + z1] = f->S ? f->S[z * p->nz + z1] : 0.0;
+  }
+  auto need = [&](const double* q, const char* what) -> bool {
+    if (q) return true;
+    fail(PQG_ERR_INVALID, std::string("diagnostic needs the field ") + what);
+    return false;
+  };
+  bool ok = true;
+  switch (kind) {
+    case PQG_DIAG_ENSSPEC: case PQG_DIAG_ENTSPEC: ok = need(f->qh, "qh"); break;
+    case PQG_DIAG_KESPEC: case PQG_DIAG_KEFRICTIONSPEC: case PQG_DIAG_APESPEC: case PQG_DIAG_APEGEN:
+      ok = need(f->ph, "ph"); break;
+    case PQG_DIAG_DISSSPEC: case PQG_DIAG_ENSDISSSPEC:
+      ok = need(f->qh, "qh") && need(f->ph, "ph") && need(f->dqhdt, "dqhdt") && need(f->dqhdt_p, "dqhdt_p") &&
+           need(f->dqhdt_pp, "dqhdt_pp");
+      break;
+    case PQG_DIAG_ENSFLUX: ok = need(f->qh, "qh") && need(f->Jq, "Jq"); break;
+    case PQG_DIAG_ENSFRICTIONSPEC: ok = need(f->qh, "qh") && need(f->ph, "ph"); break;
+    case PQG_DIAG_ENSGENSPEC: case PQG_DIAG_APEGENSPEC: ok = need(f->ph, "ph") && need(f->Sph, "Sph"); break;
+    case PQG_DIAG_KEFLUX: case PQG_DIAG_KEFLUX_DIV: ok = need(f->ph, "ph") && need(f->Jpxi, "Jpxi"); break;
+    case PQG_DIAG_APEFLUX: ok = need(f->ph, "ph") && need(f->Jptpc, "Jptpc"); break;
+    case PQG_DIAG_APEFLUX_DIV: ok = need(f->ph, "ph") && need(f->JSp, "JSp"); break;
+    case PQG_DIAG_KESPEC_MODAL: case PQG_DIAG_PESPEC_MODAL: ok = need(f->phn, "phn"); break;
+    case PQG_DIAG_EKE: case PQG_DIAG_EKEDISS: ok = need(f->u, "u") && need(f->v, "v"); break;
+    default: ok = need(f->ph, "ph") && need(f->qh, "qh"); break;
+  }
+  if (!ok) return PQG_ERR_INVALID;
+  if ((kind == PQG_DIAG_KEFLUX || kind == PQG_DIAG_APEFLUX || kind == PQG_DIAG_APEGEN) && p->nz != 2)
+    return fail(PQG_ERR_INVALID, "two-layer diagnostic on a model with nz != 2");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == PQG_DIAG_EKE || kind == PQG_DIAG_EKEDISS || kind == PQG_DIAG_APEGEN) {
+    k_diag_sum<<<152, 256, 0, st>>>(P, *f, p->kk, acc);
+  } else {
+    const int n = p->ny * p->nk;
+    k_diag_spec<<<(n + 255) / 256, 256, 0, st>>>(P, *f, p->a, p->kk, p->ll, p->k2l2, p->filtr, acc);
+  }
+  CHECK_LAUNCH();
+  return PQG_OK;
+}
+
 }  // extern "C"

@@ -139,21 +139,21 @@ class LayeredModel(qg_diagnostics.QGDiagnostics):
     def _initialize_model_diagnostics(self):
         super()._initialize_model_diagnostics()
         add = self.add_diagnostic
-        add('KEspec_modal', description='modal kinetic energy spectra',
+        add('KEspec_modal', gpu=True, description='modal kinetic energy spectra',
             function=lambda m: m.wv2 * (np.abs(m.phn) ** 2) / m.M ** 2,
             units='m^2 s^-2', dims=('lev', 'l', 'k'))
-        add('PEspec_modal', description='modal potential energy spectra',
+        add('PEspec_modal', gpu=True, description='modal potential energy spectra',
             function=lambda m: m.kdi2[1:, np.newaxis, np.newaxis] *
             (np.abs(m.phn[1:, :, :]) ** 2) / m.M ** 2,
             units='m^2 s^-2', dims=('lev_mid', 'l', 'k'))
-        add('APEspec', description='available potential energy spectrum',
+        add('APEspec', gpu=True, description='available potential energy spectrum',
             function=lambda m: (m.f2gpi * np.abs(m.ph[:-1] - m.ph[1:]) ** 2).sum(axis=0)
             / m.H / m.M ** 2,
             units='m^2 s^-2', dims=('l', 'k'))
-        add('KEflux_div', description='spectral divergence of flux of kinetic energy',
+        add('KEflux_div', gpu=True, description='spectral divergence of flux of kinetic energy',
             function=lambda m: m._layer_sum((m.ph.conj() * m.Jpxi).real) / m.M ** 2,
             units='m^2 s^-3', dims=('l', 'k'), sums_with=['paramspec_KEflux'])
-        add('APEflux_div',
+        add('APEflux_div', gpu=True,
             description='spectral divergence of flux of available potential energy',
             function=lambda m: m._layer_sum((m.ph.conj() * m.JSp).real) / m.M ** 2,
             units='m^2 s^-3', dims=('l', 'k'), sums_with=['paramspec_APEflux'])

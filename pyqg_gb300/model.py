@@ -24,6 +24,26 @@ __all__ = ["Model"]
 _MAX_BATCH = 4096
 
 
+class _DiagEntry(dict):
+    """A diagnostics entry.  Built-in diagnostics accumulate on the device
+    (key '_acc'); reading 'value' returns the host copy of the sum, as the
+    reference's entries hold it."""
+
+    def __getitem__(self, key):
+        if key == 'value' and '_acc' in self:
+            acc = dict.__getitem__(self, '_acc').cpu().numpy()
+            return acc[()] if acc.ndim == 0 else acc
+        return dict.__getitem__(self, key)
+
+    def __contains__(self, key):
+        if key == 'value' and dict.__contains__(self, '_acc'):
+            return True
+        return dict.__contains__(self, key)
+
+    def get(self, key, default=None):
+        return self[key] if key in self else default
+
+
 def grid_constants(nx, ny, L, W):
     """Spatial and spectral grids (``pyqg/model.py:446-482``).
 
@@ -338,6 +358,9 @@ class Model(PseudoSpectralKernel):
     # ------------------------------------------------------------------
     # diagnostics registry (pyqg/model.py:630-820)
     # ------------------------------------------------------------------
+    #: built-in diagnostics accumulate on the GPU (False: host functions)
+    gpu_diagnostics = True
+
     def _initialize_diagnostics(self, diagnostics_list):
         self.diagnostics = dict()
         self._initialize_core_diagnostics()
@@ -375,33 +398,33 @@ class Model(PseudoSpectralKernel):
     def _initialize_core_diagnostics(self):
         M2 = lambda m: m.M ** 2
         add = self.add_diagnostic
-        add('Ensspec', description='enstrophy spectrum',
+        add('Ensspec', gpu=True, description='enstrophy spectrum',
             function=lambda m: np.abs(m.qh) ** 2 / M2(m),
             units='s^-2', dims=('lev', 'l', 'k'))
-        add('KEspec', description='kinetic energy spectrum',
+        add('KEspec', gpu=True, description='kinetic energy spectrum',
             function=lambda m: m.wv2 * np.abs(m.ph) ** 2 / M2(m),
             units='m^2 s^-2', dims=('lev', 'l', 'k'))
-        add('EKEdiss', description='total energy dissipation by bottom drag',
+        add('EKEdiss', gpu=True, description='total energy dissipation by bottom drag',
             function=lambda m: m.Hi[-1] / m.H * m.rek * (m.v[-1] ** 2 + m.u[-1] ** 2).mean(),
             units='m^2 s^-3', dims=('time',))
-        add('KEfrictionspec', description='total energy dissipation spectrum by bottom drag',
+        add('KEfrictionspec', gpu=True, description='total energy dissipation spectrum by bottom drag',
             function=lambda m: -m.rek * m.Hi[-1] / m.H * m.wv2 * np.abs(m.ph[-1]) ** 2 / M2(m),
             units='m^2 s^-3', dims=('l', 'k'))
-        add('EKE', description='mean eddy kinetic energy',
+        add('EKE', gpu=True, description='mean eddy kinetic energy',
             function=lambda m: 0.5 * (m.v ** 2 + m.u ** 2).mean(axis=-1).mean(axis=-1),
             units='m^2 s^-2', dims=('lev',))
-        add('Dissspec', description='Spectral contribution of filter dissipation to total energy',
+        add('Dissspec', gpu=True, description='Spectral contribution of filter dissipation to total energy',
             function=lambda m: -np.tensordot(m.Hi, np.conj(m.ph) * m._filter_dissipation(),
                                              axes=(0, 0)).real / m.H / m.dt / M2(m),
             units='m^2 s^-3', dims=('l', 'k'))
-        add('ENSDissspec', description='Spectral contribution of filter dissipation to barotropic enstrophy',
+        add('ENSDissspec', gpu=True, description='Spectral contribution of filter dissipation to barotropic enstrophy',
             function=lambda m: np.tensordot(m.Hi, np.conj(m.qh) * m._filter_dissipation(),
                                             axes=(0, 0)).real / m.H / m.dt / M2(m),
             units='s^-3', dims=('l', 'k'))
-        add('paramspec', description='Spectral contribution of subgrid parameterization to energy (if present)',
+        add('paramspec', gpu=True, description='Spectral contribution of subgrid parameterization to energy (if present)',
             function=lambda m: m._calc_parameterization_spectrum(),
             units='m^2 s^-3', dims=('l', 'k'), skip_comparison=True)
-        add('ENSparamspec', description='Spectral contribution of subgrid parameterization to enstrophy',
+        add('ENSparamspec', gpu=True, description='Spectral contribution of subgrid parameterization to enstrophy',
             function=lambda m: m._calc_parameterization_enstrophy_spectrum(),
             units='s^-3', dims=('l', 'k'), skip_comparison=True)
 
@@ -437,8 +460,8 @@ class Model(PseudoSpectralKernel):
                        units=None, dims=None, **kw):
         assert hasattr(function, '__call__')
         assert isinstance(diag_name, str)
-        entry = dict(description=description, units=units, dims=dims,
-                     active=True, count=0, function=function)
+        entry = _DiagEntry(description=description, units=units, dims=dims,
+                           active=True, count=0, function=function)
         entry.update(**kw)
         self.diagnostics[diag_name] = entry
 
@@ -449,16 +472,146 @@ class Model(PseudoSpectralKernel):
             print('{:<10} | {:<54}'.format(name, self.diagnostics[name]['description']))
 
     def _increment_diagnostics(self):
-        self._calc_derived_fields()
-        for name, d in self.diagnostics.items():
-            if not d['active']:
-                continue
-            value = d['function'](self)
-            if d['count'] == 0:
-                d['value'] = value
-            else:
-                d['value'] += value
+        """Accumulate the active diagnostics.  Built-in diagnostics (those
+        registered with a device kind) accumulate in FP64 on the GPU
+        (``pqg_diag_accumulate``); the others run their host function."""
+        device = [(n, d) for n, d in self.diagnostics.items()
+                  if d['active'] and d.get('gpu') is not None and self.gpu_diagnostics]
+        host = [(n, d) for n, d in self.diagnostics.items()
+                if d['active'] and not (d.get('gpu') is not None and self.gpu_diagnostics)]
+        if device:
+            self._accumulate_device_diagnostics(device)
+        if host:
+            self._calc_derived_fields()
+            for name, d in host:
+                value = d['function'](self)
+                if d['count'] == 0:
+                    d['value'] = value
+                else:
+                    d['value'] += value
+                d['count'] += 1
+
+    # device kinds of the built-in diagnostics (enum order of the C ABI)
+    _DIAG_KIND = {name: i for i, name in enumerate((
+        'Ensspec', 'KEspec', 'EKE', 'EKEdiss', 'KEfrictionspec', 'Dissspec', 'ENSDissspec',
+        'paramspec', 'ENSparamspec', 'entspec', 'paramspec_APEflux', 'paramspec_KEflux',
+        'ENSflux', 'ENSgenspec', 'ENSfrictionspec', 'APEgenspec', 'APEflux', 'KEflux', 'APEgen',
+        'KEspec_modal', 'PEspec_modal', 'APEspec', 'KEflux_div', 'APEflux_div'))}
+    _DIAG_NEEDS = {'ENSflux': ('Jq',), 'KEflux': ('Jpxi',), 'KEflux_div': ('Jpxi',),
+                   'APEflux': ('Jptpc',), 'APEflux_div': ('JSp',), 'ENSgenspec': ('Sph',),
+                   'APEgenspec': ('Sph',), 'KEspec_modal': ('phn',), 'PEspec_modal': ('phn',)}
+
+    def _diag_shape(self, name):
+        nz, nl, nk = self.nz, self.nl, self.nk
+        if name in ('Ensspec', 'KEspec', 'KEspec_modal'):
+            return (nz, nl, nk)
+        if name == 'PEspec_modal':
+            return (nz - 1, nl, nk)
+        if name == 'EKE':
+            return (nz,)
+        if name in ('EKEdiss', 'APEgen'):
+            return ()
+        return (nl, nk)
+
+    def _device_derived(self, needs):
+        """Derived fields of the diagnostics, on the device (the device
+        counterpart of ``_calc_derived_fields``)."""
+        import torch
+        f = {}
+        ph = self.device_field("ph")
+        u, v = self.device_field("u"), self.device_field("v")
+        with torch.cuda.stream(self._stream):
+            if 'Jq' in needs:
+                f['Jq'] = self._device_advect(self.device_field("q"), u, v)
+            if 'Jpxi' in needs:
+                wv2 = torch.from_numpy(np.ascontiguousarray(self.wv2)).to(self._device)
+                xi = self._device_irfft2(-wv2 * ph)
+                f['Jpxi'] = self._device_advect(xi, u, v)
+            if 'Jptpc' in needs:
+                p = self._device_irfft2(ph)
+                f['Jptpc'] = -self._device_advect(
+                    (p[0] - p[1])[None], (self.del1 * u[0] + self.del2 * u[1])[None],
+                    (self.del1 * v[0] + self.del2 * v[1])[None])[0]
+            if 'Sph' in needs or 'JSp' in needs:
+                S = torch.from_numpy(np.ascontiguousarray(self.S, dtype=np.float64)).to(self._device)
+                f['Sph'] = torch.einsum("ij,jkl->ikl", S.to(ph.dtype), ph).contiguous()
+                if 'JSp' in needs:
+                    f['JSp'] = self._device_advect(self._device_irfft2(f['Sph']), u, v)
+            if 'phn' in needs:
+                pinv = torch.from_numpy(np.ascontiguousarray(np.linalg.inv(self.pmodes))).to(self._device)
+                f['phn'] = torch.einsum("ij,jkl->ikl", pinv.to(ph.dtype), ph).contiguous()
+        return f
+
+    def _accumulate_device_diagnostics(self, items):
+        import ctypes
+        import torch
+        from . import _lib
+        needs = set()
+        for name, _ in items:
+            needs.update(self._DIAG_NEEDS.get(name, ()))
+        derived = self._device_derived(needs)
+        keep = []
+
+        def ptr(t):
+            if t is None:
+                return None
+            keep.append(t)
+            return ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_double))
+
+        def harr(x, n):
+            if x is None:
+                return None
+            a = np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64).ravel(), (n,)))
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+        nz = self.nz
+        dt1, dt2, dt3 = self._ab_coefficients()
+        fl = _lib.DiagFields()
+        fl.qh = ptr(self.device_field("qh"))
+        fl.ph = ptr(self.device_field("ph"))
+        fl.dqhdt = ptr(self.device_field("dqhdt"))
+        fl.dqhdt_p = ptr(self.device_field("dqhdt_p"))
+        fl.dqhdt_pp = ptr(self.device_field("dqhdt_pp"))
+        fl.u = ptr(self.device_field("u"))
+        fl.v = ptr(self.device_field("v"))
+        for key in ('Jq', 'Jpxi', 'Jptpc', 'JSp', 'Sph', 'phn'):
+            setattr(fl, key, ptr(derived.get(key)))
+        if self.q_parameterization is not None:
+            fl.dqh = ptr(self.device_field("dqh"))
+        if self.uv_parameterization is not None:
+            fl.duh = ptr(self.device_field("duh"))
+            fl.dvh = ptr(self.device_field("dvh"))
+        fl.H = float(getattr(self, 'H', 1.0))
+        fl.dt, fl.c1, fl.c2, fl.c3 = float(self.dt), float(dt1), float(dt2), float(dt3)
+        for key in ('rd', 'del1', 'del2', 'U'):
+            val = getattr(self, key, None)
+            setattr(fl, key, float(val) if np.isscalar(val) and val is not None else 0.0)
+        fl.Hi = harr(getattr(self, 'Hi', np.ones(nz)), nz)
+        fl.Qx = harr(getattr(self, 'Qx', 0.0) if np.ndim(getattr(self, 'Qx', 0.0)) <= 1 else 0.0, nz)
+        fl.Qy = harr(self.Qy, nz)
+        fl.Ubg = harr(self.Ubg, nz)
+        fl.Vbg = harr(getattr(self, 'Vbg', 0.0), nz)
+        if hasattr(self, 'f2gpi'):
+            fl.f2gpi = harr(np.ravel(self.f2gpi), max(1, np.size(self.f2gpi)))
+        if hasattr(self, 'kdi2'):
+            fl.kdi2 = harr(self.kdi2, nz)
+        if hasattr(type(self), 'S') or hasattr(self, 'S'):
+            try:
+                fl.S = harr(np.asarray(self.S, dtype=np.float64), nz * nz)
+            except Exception:
+                fl.S = None
+        L = self._L
+        for name, d in items:
+            acc = d.get('_acc')
+            if acc is None:
+                acc = torch.zeros(self._diag_shape(name), dtype=torch.float64, device=self._device)
+                dict.__setitem__(d, '_acc', acc)
+            _lib.check(L.pqg_diag_accumulate(self._plan, self._DIAG_KIND[name], ctypes.byref(fl),
+                                             acc.data_ptr(), self._sp()))
             d['count'] += 1
+        if keep:
+            torch.cuda.current_stream().wait_stream(self._stream)
 
     def get_diagnostic(self, dname):
         d = self.diagnostics[dname]

@@ -15,33 +15,33 @@ class QGDiagnostics(model.Model):
     def _initialize_model_diagnostics(self):
         M2 = self.M ** 2
         add = self.add_diagnostic
-        add('entspec', description='barotropic enstrophy spectrum',
+        add('entspec', gpu=True, description='barotropic enstrophy spectrum',
             function=lambda m: np.abs(m._layer_sum(m.qh)) ** 2 / m.M ** 2,
             units='m s^-2', dims=('l', 'k'))
-        add('paramspec_APEflux',
+        add('paramspec_APEflux', gpu=True,
             description='total additional APE flux due to subgrid parameterization',
             function=lambda m: -m._calc_paramspec_contribution(np.einsum(
                 "ij, jk..., k... -> i...", m.S, m.a,
                 m._calc_parameterization_contribution())),
             units='m^2 s^-3', dims=('l', 'k'), skip_comparison=True)
-        add('paramspec_KEflux',
+        add('paramspec_KEflux', gpu=True,
             description='total additional KE flux due to subgrid parameterization',
             function=lambda m: m.wv2 * m._calc_paramspec_contribution(np.einsum(
                 "ij..., j... -> i...", m.a, m._calc_parameterization_contribution())),
             units='m^2 s^-3', dims=('l', 'k'), skip_comparison=True)
-        add('ENSflux', description='barotropic enstrophy flux',
+        add('ENSflux', gpu=True, description='barotropic enstrophy flux',
             function=lambda m: -m._layer_sum((m.qh.conj() * m.Jq).real) / m.M ** 2,
             units='s^-3', dims=('l', 'k'))
-        add('ENSgenspec',
+        add('ENSgenspec', gpu=True,
             description='the spectrum of the rate of generation of barotropic enstrophy',
             function=lambda m: m._layer_sum(((m.ilQx - m.ikQy) * m.Sph.conj() * m.ph).real) / m.M ** 2,
             units='s^-3', dims=('l', 'k'))
-        add('ENSfrictionspec',
+        add('ENSfrictionspec', gpu=True,
             description='the spectrum of the rate of dissipation of barotropic enstrophy due to bottom friction',
             function=lambda m: m.rek * m.Hi[-1] / m.H * m.wv2 *
             (m.qh[-1].conj() * m.ph[-1]).real / m.M ** 2,
             units='s^-3', dims=('l', 'k'))
-        add('APEgenspec',
+        add('APEgenspec', gpu=True,
             description='the spectrum of the rate of generation of available potential energy',
             function=lambda m: m._layer_sum(
                 (m.Ubg[:, np.newaxis, np.newaxis] * m.k + m.Vbg[:, np.newaxis, np.newaxis] * m.l) *

@@ -102,15 +102,15 @@ class QGModel(qg_diagnostics.QGDiagnostics):
     def _initialize_model_diagnostics(self):
         super()._initialize_model_diagnostics()
         add = self.add_diagnostic
-        add('APEflux', description='spectral flux of available potential energy',
+        add('APEflux', gpu=True, description='spectral flux of available potential energy',
             function=lambda m: m.rd ** -2 * m.del1 * m.del2 *
             np.real((m.ph[0] - m.ph[1]) * np.conj(m.Jptpc)) / m.M ** 2,
             units='m^2 s^-3', dims=('l', 'k'), sums_with=['paramspec_APEflux'])
-        add('KEflux', description='spectral flux of kinetic energy',
+        add('KEflux', gpu=True, description='spectral flux of kinetic energy',
             function=lambda m: (np.real(m.del1 * m.ph[0] * np.conj(m.Jpxi[0])) +
                                 np.real(m.del2 * m.ph[1] * np.conj(m.Jpxi[1]))) / m.M ** 2,
             units='m^2 s^-3', dims=('l', 'k'), sums_with=['paramspec_KEflux'])
-        add('APEgen', description='total available potential energy generation',
+        add('APEgen', gpu=True, description='total available potential energy generation',
             function=lambda m: m._ape_generation(),
             units='m^2 s^-3', dims=('time',))
 
