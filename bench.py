@@ -451,6 +451,24 @@ def closure_throughput(args, plain_value):
     return res
 
 
+def profile_case(args):
+    """Small workloads for profiler captures (no timing, no output line)."""
+    import torch
+    import pyqg_gb300 as P
+    if args.profile_step:
+        m = P.QGModel(nx=args.nx, dt=3600.0, **C2, **QUIET)
+        m.q = 1e-7 * np.random.default_rng(0).standard_normal((2, args.nx, args.nx))
+        m._step_fused(args.profile_step)
+    if args.profile_cnn:
+        from pyqg_gb300.closure import ConvNet
+        net = ConvNet(max_batch=args.profile_cnn, seed=0)
+        x = torch.randn(args.profile_cnn, 2, 64, 64, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(2):
+            net.forward(x, y)
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -464,7 +482,14 @@ def main():
     ap.add_argument("--closure-steps", type=int, default=5)
     ap.add_argument("--closure-chunk", type=int, default=100)
     ap.add_argument("--no-closure", action="store_true", help="skip the closure-ensemble measurement")
+    ap.add_argument("--profile-step", type=int, default=0, metavar="N",
+                    help="only run N fused nx=256 steps (a small case for profilers) and exit")
+    ap.add_argument("--profile-cnn", type=int, default=0, metavar="B",
+                    help="only run two closure-network forwards of a batch of B and exit")
     args = ap.parse_args()
+    if args.profile_step or args.profile_cnn:
+        profile_case(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -333,8 +333,16 @@ class PseudoSpectralKernel:
                     x = np.broadcast_to(x, dst.shape)
                 dst.copy_(torch.from_numpy(np.ascontiguousarray(x)))
 
+    def _call_hook(self, hook):
+        """Run a parameterization with device outputs allowed."""
+        self._hook_on_device = True
+        try:
+            return hook(self)
+        finally:
+            self._hook_on_device = False
+
     def _do_q_subgrid_parameterization(self):
-        dq = self.q_parameterization(self)
+        dq = self._call_hook(self.q_parameterization)
         self._sync_in()
         self._to_device_field("dq", dq)
         self._own("dqhdt", copy=True)
@@ -343,7 +351,7 @@ class PseudoSpectralKernel:
                                             self._sp()))
 
     def _do_uv_subgrid_parameterization(self):
-        res = self.uv_parameterization(self)
+        res = self._call_hook(self.uv_parameterization)
         du, dv = res[0], res[1]
         self._sync_in()
         self._to_device_field("du", du)
