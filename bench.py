@@ -378,6 +378,11 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks.summary(),
         "gpu_launches": args.steps * (2 * args.chunk + 2),
     }
+    if world == 1 and not args.no_ensemble:
+        try:
+            line["ensemble"] = ensemble_throughput(args)
+        except Exception as exc:
+            line["ensemble"] = {"error": "%s: %s" % (type(exc).__name__, exc)}
     if world == 1 and not args.no_closure:
         try:
             line["closure"] = closure_throughput(args, value)
@@ -451,6 +456,53 @@ def closure_throughput(args, plain_value):
     return res
 
 
+def ensemble_throughput(args):
+    """Config-3 workload: 1024 FP32 members of uneven size (614 x nx=64,
+    307 x nx=128, 103 x nx=256; 20 % three-layer), beta and rek drawn per
+    member, autotuned launch shapes, groups on concurrent branches and
+    steady-state stretches replayed as CUDA graphs."""
+    import torch
+    import pyqg_gb300 as P
+    rng = np.random.default_rng(1234)
+    members = []
+    for nx, cnt in ((64, 614), (128, 307), (256, 103)):
+        dt = 3600.0 if nx == 256 else 7200.0
+        for i in range(cnt):
+            beta = rng.uniform(0.5, 2) * 1.5e-11
+            rek = rng.uniform(0.5, 2) * 5.787e-7
+            if i < int(0.2 * cnt + 0.5):
+                members.append(("layered", dict(nx=nx, dt=dt, nz=3, H=[500., 1000., 2500.],
+                                                U=[0.05, 0.02, 0.0], V=[0., 0., 0.], beta=beta, rek=rek)))
+            else:
+                members.append(("qg", dict(nx=nx, dt=dt, beta=beta, rek=rek)))
+    ens = P.Ensemble(members, precision="fp32")
+    qs = [1e-7 * rng.standard_normal((3 if k == "layered" else 2, kw["nx"], kw["nx"])) for k, kw in members]
+    ens.set_q(qs)
+    ens.step(4)
+    ens.autotune()
+    stream = torch.cuda.current_stream()
+    nsteps = args.ensemble_steps
+    ens.step(32)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ens.step(nsteps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / nsteps
+    S = sum(g.B * g.nz * g.nx * (g.nx // 2 + 1) for g in ens.groups)
+    Pn = sum(g.B * g.nz * g.nx * g.nx for g in ens.groups)
+    nbytes = 40 * S + 8 * Pn
+    hbm, kind = peaks()
+    ach = nbytes / (ms * 1e-3) / 1e9
+    return {"workload": "config 3: 1024 FP32 members (614 x nx=64, 307 x nx=128, 103 x nx=256, "
+                        "20 % three-layer), uneven beta / rek, autotuned, CUDA graphs",
+            "ms_per_ensemble_step": ms, "member_steps_per_s": len(members) / (ms * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                         "algorithmic_bytes_per_step": nbytes, "peak_source": kind,
+                         "note": "compulsory bytes 40 S + 8 P (FP32) per ensemble step"}}
+
+
 def profile_case(args):
     """Small workloads for profiler captures (no timing, no output line)."""
     import torch
@@ -482,6 +534,8 @@ def main():
     ap.add_argument("--closure-steps", type=int, default=5)
     ap.add_argument("--closure-chunk", type=int, default=100)
     ap.add_argument("--no-closure", action="store_true", help="skip the closure-ensemble measurement")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the config-3 ensemble measurement")
+    ap.add_argument("--ensemble-steps", type=int, default=200)
     ap.add_argument("--profile-step", type=int, default=0, metavar="N",
                     help="only run N fused nx=256 steps (a small case for profilers) and exit")
     ap.add_argument("--profile-cnn", type=int, default=0, metavar="B",

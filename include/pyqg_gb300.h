@@ -185,8 +185,16 @@ int pqg_ens_set_q(pqg_ens *ens, const double *q, void *stream);
 int pqg_ens_get_q(pqg_ens *ens, double *q, void *stream);
 int pqg_ens_step(pqg_ens *ens, int nsteps, void *stream);
 /* several ensembles (e.g. one per grid size), each on its own stream
- * branch so that they overlap on the GPU */
+ * branch so that they overlap on the GPU.  Steady-state stretches of 16
+ * steps are captured once into a CUDA graph and replayed (environment
+ * PQG_ENS_NO_GRAPHS=1 disables this). */
 int pqg_ens_step_many(pqg_ens **ens, int count, int nsteps, void *stream);
+/* autotuner: times the row kernel over (rows per CTA, threads) and the
+ * fused column kernel over (columns per CTA, threads) on the ensemble's own
+ * state, keeps the fastest and restores the state; out (may be NULL) gets
+ * {rows per CTA, row threads, row ms, columns per CTA, column threads,
+ * column ms}.  Synchronizes `stream`. */
+int pqg_ens_autotune(pqg_ens *ens, double *out, void *stream);
 /* FP64 sums per (member, layer): ke = 0.5 sum |kappa ph|^2 / M^2 and
  * enstrophy 0.5 sum |qh|^2 / M^2 over the full spectral plane (host out) */
 int pqg_ens_energy(pqg_ens *ens, double *ke, double *enstrophy, void *stream);

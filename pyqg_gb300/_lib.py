@@ -84,6 +84,7 @@ SIGNATURES = {
     "pqg_ens_step_many": (_I, [ctypes.POINTER(_P), _I, _I, _P]),
     "pqg_ens_energy": (_I, [_P, _P, _P, _P]),
     "pqg_ens_set_closure": (_I, [_P, _P]),
+    "pqg_ens_autotune": (_I, [_P, _P, _P]),
     "pqg_ens_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
                            ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_D)]),
     "pqg_advect": (_I, [_P, _P, _P, _P, _I, _P, _P]),

@@ -444,6 +444,7 @@ struct pqg_ens {
   double t = 0.0, dt = 0.0;
   int T_row = 128, rb = 1, T_col = 128, C = 1;
   int nfield = 3;               // mixed planes per member: U, V, Q (+ forcing F)
+  long long version = 0;        // bumped when launch parameters change (graph cache key)
   pqg_cnn* net = nullptr;       // closure: forcing = net(q) every step
   void* qcur = nullptr;         // physical q of the current step (closure input)
   void* dqf = nullptr;          // closure output, physical
@@ -452,6 +453,8 @@ struct pqg_ens {
 };
 
 namespace {
+
+void drop_graphs_of(pqg_ens* e);   // graph cache (defined with the step entry points)
 
 void cos_sin(int n, int m, long double& cr, long double& sr) {
   const long double pi = 3.141592653589793238462643383279502884L;
@@ -745,6 +748,7 @@ PQG_API int pqg_ens_create(pqg_ens** out, int nmembers, int nz, int ny, int nx, 
 
 PQG_API int pqg_ens_destroy(pqg_ens* e) {
   if (!e) return PQG_OK;
+  drop_graphs_of(e);
   void* ps[] = {e->twx, e->twy, e->a, e->kk, e->ll, e->k2l2, e->filtr, e->kQy, e->Ubg, e->rek, e->q,
                 e->qh, e->dq[0], e->dq[1], e->dq[2], e->scratch, e->d_red, e->qcur, e->dqf};
   for (void* p : ps) cudaFree(p);
@@ -754,6 +758,10 @@ PQG_API int pqg_ens_destroy(pqg_ens* e) {
 
 PQG_API int pqg_ens_set_constants(pqg_ens* e, const double* a, const double* kk, const double* ll,
                                   const double* filtr, double dt) {
+  if (e) {
+    e->version++;     // dt enters the captured AB coefficients
+    drop_graphs_of(e);
+  }
   if (!e || !a || !kk || !ll || !filtr) return efail(PQG_ERR_INVALID, "NULL argument");
   const int nk = e->nk, ny = e->ny, nz = e->nz;
   // device copies are k-major: (.., nk, ny)
@@ -834,12 +842,12 @@ PQG_API int pqg_ens_step(pqg_ens* e, int nsteps, void* stream) {
                       : step_impl<double2>(e, nsteps, (cudaStream_t)stream);
 }
 
-// All groups advance `nsteps` steps; each group on its own captured stream
-// branch so that groups overlap on the GPU; replayed as one graph per call.
-PQG_API int pqg_ens_step_many(pqg_ens** es, int count, int nsteps, void* stream) {
-  if (!es || count < 1 || nsteps < 0) return efail(PQG_ERR_INVALID, "bad argument to pqg_ens_step_many");
-  cudaStream_t st = (cudaStream_t)stream;
-  if (count == 1) return pqg_ens_step(es[0], nsteps, stream);
+}  // extern "C"
+
+// groups on their own stream branches (fork / join through events), so that
+// groups overlap on the GPU
+static int run_many(pqg_ens** es, int count, int nsteps, cudaStream_t st) {
+  if (count == 1) return pqg_ens_step(es[0], nsteps, st);
   std::vector<cudaStream_t> br(count);
   std::vector<cudaEvent_t> done(count);
   cudaEvent_t fork;
@@ -864,6 +872,216 @@ PQG_API int pqg_ens_step_many(pqg_ens** es, int count, int nsteps, void* stream)
   return rc;
 }
 
+// CUDA graphs of K steps of a set of ensembles in the steady state
+// (ablevel 2).  K is even, so the history roles return to their captured
+// assignment after every replay; the key holds the ensembles, their
+// versions and roles.
+namespace {
+constexpr int kGraphSteps = 16;
+struct EnsGraph {
+  std::vector<pqg_ens*> ens;
+  std::vector<long long> ver;
+  std::vector<int> role;
+  cudaGraphExec_t exec = nullptr;
+};
+std::vector<EnsGraph> g_ens_graphs;
+cudaStream_t g_cap_stream = nullptr;
+
+bool graph_matches(const EnsGraph& g, pqg_ens** es, int count) {
+  if ((int)g.ens.size() != count) return false;
+  for (int i = 0; i < count; i++)
+    if (g.ens[i] != es[i] || g.ver[i] != es[i]->version || g.role[i] != es[i]->role_p) return false;
+  return true;
+}
+
+void drop_graphs_of(pqg_ens* e) {
+  for (size_t i = 0; i < g_ens_graphs.size();) {
+    bool hit = false;
+    for (auto* x : g_ens_graphs[i].ens) hit |= x == e;
+    if (hit) {
+      cudaGraphExecDestroy(g_ens_graphs[i].exec);
+      g_ens_graphs.erase(g_ens_graphs.begin() + i);
+    } else {
+      i++;
+    }
+  }
+}
+}  // namespace
+
+static int graph_for(pqg_ens** es, int count, cudaGraphExec_t* out) {
+  for (auto& g : g_ens_graphs)
+    if (graph_matches(g, es, count)) { *out = g.exec; return PQG_OK; }
+  if (!g_cap_stream) ECUDA(cudaStreamCreateWithFlags(&g_cap_stream, cudaStreamNonBlocking));
+  // capturing runs the host bookkeeping of K steps without executing them:
+  // save it and put it back afterwards
+  struct Host { int rp, rpp, ab; long long tc; double t; };
+  std::vector<Host> h(count);
+  for (int i = 0; i < count; i++) h[i] = {es[i]->role_p, es[i]->role_pp, es[i]->ablevel, es[i]->tc, es[i]->t};
+  ECUDA(cudaStreamBeginCapture(g_cap_stream, cudaStreamCaptureModeThreadLocal));
+  int rc = run_many(es, count, kGraphSteps, g_cap_stream);
+  cudaGraph_t graph = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(g_cap_stream, &graph);
+  for (int i = 0; i < count; i++) {
+    es[i]->role_p = h[i].rp;
+    es[i]->role_pp = h[i].rpp;
+    es[i]->ablevel = h[i].ab;
+    es[i]->tc = h[i].tc;
+    es[i]->t = h[i].t;
+  }
+  if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (ce != cudaSuccess) return efail(PQG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+  EnsGraph g;
+  ce = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) return efail(PQG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+  for (int i = 0; i < count; i++) {
+    g.ens.push_back(es[i]);
+    g.ver.push_back(es[i]->version);
+    g.role.push_back(es[i]->role_p);
+  }
+  if (g_ens_graphs.size() >= 16) {
+    cudaGraphExecDestroy(g_ens_graphs.front().exec);
+    g_ens_graphs.erase(g_ens_graphs.begin());
+  }
+  g_ens_graphs.push_back(g);
+  *out = g.exec;
+  return PQG_OK;
+}
+
+extern "C" {
+
+// All groups advance `nsteps` steps.  Start-up steps (FE, AB2) run as plain
+// launches; steady-state stretches of 16 steps replay a captured graph
+// (PQG_ENS_NO_GRAPHS=1 disables the graphs).
+PQG_API int pqg_ens_step_many(pqg_ens** es, int count, int nsteps, void* stream) {
+  if (!es || count < 1 || nsteps < 0) return efail(PQG_ERR_INVALID, "bad argument to pqg_ens_step_many");
+  for (int i = 0; i < count; i++)
+    if (!es[i] || !es[i]->have_consts || !es[i]->have_members)
+      return efail(PQG_ERR_STATE, "constants or members not set");
+  cudaStream_t st = (cudaStream_t)stream;
+  const char* ng = getenv("PQG_ENS_NO_GRAPHS");
+  if (ng && ng[0] == '1') return run_many(es, count, nsteps, st);
+  int done = 0;
+  auto steady = [&]() {
+    for (int i = 0; i < count; i++)
+      if (es[i]->ablevel < 2) return false;
+    return true;
+  };
+  while (done < nsteps && !steady()) {
+    int rc = run_many(es, count, 1, st);
+    if (rc) return rc;
+    done++;
+  }
+  const int chunks = (nsteps - done) / kGraphSteps;
+  if (chunks > 0) {
+    cudaGraphExec_t exec;
+    int rc = graph_for(es, count, &exec);
+    if (rc) return rc;
+    for (int c = 0; c < chunks; c++) ECUDA(cudaGraphLaunch(exec, st));
+    for (int i = 0; i < count; i++) {
+      es[i]->tc += (long long)chunks * kGraphSteps;
+      es[i]->t += (double)chunks * kGraphSteps * es[i]->dt;
+    }
+    done += chunks * kGraphSteps;
+  }
+  if (done < nsteps) return run_many(es, count, nsteps - done, st);
+  return PQG_OK;
+}
+
+}  // extern "C"
+
+// --- autotuner ---------------------------------------------------------
+// Times the row kernel over (rows per CTA, threads) and the fused column
+// kernel over (columns per CTA, threads) on the ensemble's own state, keeps
+// the fastest of each and restores the state.
+template <class V>
+int autotune_impl(pqg_ens* e, cudaStream_t st, double* out) {
+  const size_t S = (size_t)e->B * e->nz * e->ny * e->nk, P = (size_t)e->B * e->nz * e->ny * e->nx;
+  const size_t vb = 2 * e->esz * S, qb = e->esz * P;
+  void* save = nullptr;
+  if (cudaMalloc(&save, 4 * vb + qb) != cudaSuccess) return efail(PQG_ERR_NOMEM, "autotune: cudaMalloc failed");
+  unsigned char* sv = (unsigned char*)save;
+  ECUDA(cudaMemcpyAsync(sv, e->qh, vb, cudaMemcpyDeviceToDevice, st));
+  for (int i = 0; i < 3; i++) ECUDA(cudaMemcpyAsync(sv + (1 + i) * vb, e->dq[i], vb, cudaMemcpyDeviceToDevice, st));
+  ECUDA(cudaMemcpyAsync(sv + 4 * vb, e->q, qb, cudaMemcpyDeviceToDevice, st));
+  const int rp = e->role_p, rpp = e->role_pp, ab = e->ablevel;
+  const long long tc = e->tc;
+  const double t = e->t;
+  const size_t limit = 200 * 1024;
+  cudaEvent_t a, b;
+  ECUDA(cudaEventCreate(&a));
+  ECUDA(cudaEventCreate(&b));
+  auto time3 = [&](auto&& launch) -> float {
+    launch();
+    cudaEventRecord(a, st);
+    for (int r = 0; r < 3; r++) launch();
+    cudaEventRecord(b, st);
+    if (cudaEventSynchronize(b) != cudaSuccess || cudaGetLastError() != cudaSuccess) return 1e30f;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms / 3;
+  };
+  int rc = launch_prologue<V>(e, st);
+  // rows
+  float best_r = 1e30f;
+  int brb = e->rb, btr = e->T_row;
+  for (int rb = 1; rb <= 16 && !rc; rb *= 2) {
+    if (e->ny % rb || vsz(e) * ((size_t)e->nx + 3 * (size_t)rb * e->M) > limit) continue;
+    for (int tr : {64, 128, 256, 512}) {
+      if (tr > 32 * ((rb * e->M + 31) / 32) * 2) continue;
+      e->rb = rb;
+      e->T_row = tr;
+      const float ms = time3([&]() { launch_row_adv<V>(e, false, st); });
+      if (ms < best_r) { best_r = ms; brb = rb; btr = tr; }
+    }
+  }
+  e->rb = brb;
+  e->T_row = btr;
+  // columns (the fused kernel updates the state: restored below)
+  float best_c = 1e30f;
+  int bc = e->C, btc = e->T_col;
+  for (int C = 1; C <= 16 && !rc; C *= 2) {
+    if (C > e->nk || vsz(e) * (size_t)e->ny * (1 + 4 * C) > limit) continue;
+    for (int tcn : {64, 128, 256, 512}) {
+      if (tcn > 2 * e->ny * C) continue;
+      e->C = C;
+      e->T_col = tcn;
+      const float ms = time3([&]() { launch_col_fused<V>(e, st); });
+      if (ms < best_c) { best_c = ms; bc = C; btc = tcn; }
+    }
+  }
+  e->C = bc;
+  e->T_col = btc;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ECUDA(cudaMemcpyAsync(e->qh, sv, vb, cudaMemcpyDeviceToDevice, st));
+  for (int i = 0; i < 3; i++) ECUDA(cudaMemcpyAsync(e->dq[i], sv + (1 + i) * vb, vb, cudaMemcpyDeviceToDevice, st));
+  ECUDA(cudaMemcpyAsync(e->q, sv + 4 * vb, qb, cudaMemcpyDeviceToDevice, st));
+  ECUDA(cudaStreamSynchronize(st));
+  cudaFree(save);
+  e->role_p = rp;
+  e->role_pp = rpp;
+  e->ablevel = ab;
+  e->tc = tc;
+  e->t = t;
+  e->version++;
+  drop_graphs_of(e);
+  if (out) {
+    out[0] = e->rb; out[1] = e->T_row; out[2] = best_r;
+    out[3] = e->C; out[4] = e->T_col; out[5] = best_c;
+  }
+  return rc;
+}
+
+extern "C" {
+
+PQG_API int pqg_ens_autotune(pqg_ens* e, double* out, void* stream) {
+  if (!e) return efail(PQG_ERR_INVALID, "NULL argument");
+  if (!e->have_consts || !e->have_members) return efail(PQG_ERR_STATE, "constants or members not set");
+  cudaStream_t st = (cudaStream_t)stream;
+  return e->prec == 4 ? autotune_impl<float2>(e, st, out) : autotune_impl<double2>(e, st, out);
+}
+
 PQG_API int pqg_ens_energy(pqg_ens* e, double* ke, double* ens, void* stream) {
   if (!e || !ke || !ens) return efail(PQG_ERR_INVALID, "NULL argument");
   cudaStream_t st = (cudaStream_t)stream;
@@ -885,6 +1103,8 @@ PQG_API int pqg_ens_energy(pqg_ens* e, double* ke, double* ens, void* stream) {
 PQG_API int pqg_ens_set_closure(pqg_ens* e, pqg_cnn* net) {
   if (!e) return efail(PQG_ERR_INVALID, "NULL argument");
   if (cudaDeviceSynchronize() != cudaSuccess) return efail(PQG_ERR_CUDA, "device error before pqg_ens_set_closure");
+  e->version++;
+  drop_graphs_of(e);
   if (!net) {
     e->net = nullptr;
     return PQG_OK;

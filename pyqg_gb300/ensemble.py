@@ -118,6 +118,14 @@ class EnsembleGroup:
         self._check(self._L.pqg_ens_energy(self._h, ke.ctypes.data, en.ctypes.data, self._sp()))
         return ke, en
 
+    def autotune(self):
+        """Pick the fastest row / column launch configuration on this
+        group's state (the state is restored); returns the choice."""
+        out = np.zeros(6)
+        self._check(self._L.pqg_ens_autotune(self._h, out.ctypes.data, self._sp()))
+        return dict(rows_per_cta=int(out[0]), row_threads=int(out[1]), row_ms=float(out[2]),
+                    cols_per_cta=int(out[3]), col_threads=int(out[4]), col_ms=float(out[5]))
+
     def set_closure(self, net):
         """Attach a :class:`~pyqg_gb300.closure.ConvNet` (or None): every step
         adds its PV forcing, as a q_parameterization would."""
@@ -208,6 +216,10 @@ class Ensemble:
                 grp.set_closure(net)
                 n += 1
         return n
+
+    def autotune(self):
+        """Autotune every group's launch configuration; returns the choices."""
+        return [g.autotune() for g in self.groups]
 
     def energy(self):
         """FP64 (ke, enstrophy) per member and layer, in member order."""

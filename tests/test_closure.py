@@ -27,6 +27,19 @@ def _torch_net(channels, params, slices, x, round_hidden=True):
     return h
 
 
+def _he_params(net, seed):
+    """He-uniform weights and small biases: a well-conditioned network for
+    checking kernels (independent of the training initialisation)."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(net.nparams, dtype=np.float32)
+    for ws, shape, bs in net.layer_slices():
+        fan_in = shape[1] * shape[2] * shape[3]
+        b = np.sqrt(6.0 / fan_in)
+        p[ws] = rng.uniform(-b, b, size=ws.stop - ws.start)
+        p[bs] = rng.uniform(-0.05, 0.05, size=bs.stop - bs.start)
+    return p
+
+
 def _reference_grads(channels, params, slices, x, t):
     import torch
     import torch.nn.functional as F
@@ -91,7 +104,7 @@ def test_gradients_match_autograd(channels, batch):
     import torch
     from pyqg_gb300.closure import ConvNet
     net = ConvNet(channels, max_batch=batch, seed=4)
-    p = net.params
+    p = _he_params(net, 4)
     rng = np.random.default_rng(1)
     p += (0.02 * rng.standard_normal(p.shape)).astype(np.float32)
     net.params = p
@@ -231,7 +244,7 @@ def test_gradients_many_tiles_per_cta():
     channels = (2, 128, 64, 32, 32, 32, 32, 32, 2)
     batch = 48
     net = ConvNet(channels, max_batch=batch, seed=8)
-    p = net.params
+    p = _he_params(net, 8)
     rng = np.random.default_rng(6)
     p += (0.02 * rng.standard_normal(p.shape)).astype(np.float32)
     net.params = p

@@ -106,3 +106,43 @@ def test_fp32_form_error_vs_fp64_oracle():
     err = rel_l2(ens.q(0), o.q)
     print("FP32 form, nx=256, 10 steps: relative L2 error on q = %.3e" % err)
     assert err < 1e-5
+
+
+def _two_groups(precision="fp64"):
+    import pyqg_gb300 as P
+    members = [("qg", dict(nx=64, dt=7200.0, beta=1.2e-11)), ("qg", dict(nx=128, dt=7200.0)),
+               ("qg", dict(nx=64, dt=7200.0, rek=3e-7))]
+    ens = P.Ensemble(members, precision=precision)
+    rng = np.random.default_rng(21)
+    ens.set_q([1e-6 * rng.standard_normal((2, kw["nx"], kw["nx"])) for _, kw in members])
+    return ens
+
+
+@pytest.mark.gpu
+def test_graph_replay_equals_plain_launches(monkeypatch):
+    a = _two_groups()
+    monkeypatch.setenv("PQG_ENS_NO_GRAPHS", "1")
+    a.step(50)
+    b = _two_groups()
+    monkeypatch.setenv("PQG_ENS_NO_GRAPHS", "0")
+    b.step(20)
+    b.step(30)          # graphs of 16 steps, then plain launches for the rest
+    for i in range(3):
+        np.testing.assert_array_equal(a.q(i), b.q(i))
+    assert a.tc == b.tc
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_the_state_and_results():
+    a = _two_groups()
+    b = _two_groups()
+    a.step(5)
+    b.step(5)
+    choices = b.autotune()
+    assert len(choices) == len(b.groups)
+    for c in choices:
+        assert c["rows_per_cta"] >= 1 and c["cols_per_cta"] >= 1 and c["col_ms"] > 0
+    a.step(40)
+    b.step(40)
+    for i in range(3):
+        np.testing.assert_array_equal(a.q(i), b.q(i))
