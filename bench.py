@@ -36,6 +36,19 @@ def sim_yr_per_hr(model_steps, dt, seconds):
     return (model_steps * dt / YEAR) / (seconds / 3600.0)
 
 
+def replica_value(local_s, model_steps, dt, world, device=None):
+    """Replicas only: every rank advances its own model; the job's time is
+    the slowest rank's (MAX over ranks) and the value sums the ranks'
+    simulated years.  Returns (value, job seconds)."""
+    total_s = local_s
+    if world > 1:
+        import torch
+        t = torch.tensor([local_s], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    return world * sim_yr_per_hr(model_steps, dt, total_s), total_s
+
+
 def peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -288,13 +301,8 @@ def run_ours(args, rank, world, local_rank):
         clocks.mark_stop()
     if world > 1:
         torch.distributed.barrier()
-    total_s = sum(ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
     model_steps = args.steps * args.chunk
-    value = world * sim_yr_per_hr(model_steps, dt, total_s)
+    value, total_s = replica_value(sum(ms) / 1e3, model_steps, dt, world, dev)
 
     # per-kernel durations (CUDA events around every launch, no graph)
     st = state()

@@ -61,6 +61,7 @@ constexpr int CHUNK_A = TM * KC * 2;   // bytes of one A stage (gather kernels)
 constexpr int TY = 16;     // output rows of a halo-kernel tile
 constexpr int TYH = TY + 2 * PAD;
 constexpr int MAXST = 2 * NTAP;   // weight stages of the halo kernel (at most one per tap and unit)
+constexpr int NEPI = 8;           // epilogue warps of the halo kernel (two per TMEM lane quarter)
 
 thread_local std::string c_last_error;
 
@@ -169,13 +170,14 @@ __device__ __forceinline__ void epilogue8(const Epi& e, const float* bias, const
 
 // ---------------------------------------------------------------------------
 // halo-tile convolution (input channels 16, 32, 64 or 128), persistent and
-// warp-specialised, one CTA per SM, 5 + SX warps:
-//   warps 0-3     epilogue: TMEM -> registers -> global (warp w owns TMEM
-//                 lanes 32w..32w+31)
-//   warp 4        producer (one lane): TMA halo tiles into `nh` buffers,
+// warp-specialised, one CTA per SM, 9 + SX warps:
+//   warps 0-7     epilogue: TMEM -> registers -> global (warp w reads TMEM
+//                 lanes 32 (w % 4) ..; the two warps of a lane quarter split
+//                 the subtiles, or the columns of a single subtile)
+//   warp 8        producer (one lane): TMA halo tiles into `nh` buffers,
 //                 per-tap weight blocks into a ring of `nst` stages (loaded
 //                 once when all 25 taps are resident)
-//   warps 5..     one MMA issuer (one lane) per 8-column subtile: 25 taps x
+//   warps 9..     one MMA issuer (one lane) per 8-column subtile: 25 taps x
 //                 cin/16 MMAs per tile into the subtile's columns of one of
 //                 two TMEM accumulators.
 // Inputs of more than 64 channels are pipelined in units of 64 channels (a
@@ -201,7 +203,7 @@ struct HaloArgs {
 };
 
 template <int SX, int KS>
-__global__ void __launch_bounds__(32 * (5 + SX)) k_conv_halo(const __grid_constant__ CUtensorMap tmap, HaloArgs a) {
+__global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid_constant__ CUtensorMap tmap, HaloArgs a) {
   constexpr int TXH = 8 * SX + 2 * PAD;
   constexpr int SLAB = TXH * TYH * 16;     // bytes per 8 channels
   constexpr int CH = KS > 4 ? KS / 4 : 1;  // channel units per tile
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(32 * (5 + SX)) k_conv_halo(const __grid_consta
       tc::mbar_init(&hfull[i], 1);
       tc::mbar_init(&hempty[i], SX);
       tc::mbar_init(&afull[i], SX);
-      tc::mbar_init(&aempty[i], 128);
+      tc::mbar_init(&aempty[i], 32 * NEPI);
     }
     for (int s = 0; s < NST; s++) {
       tc::mbar_init(&wfull[s], 1);
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(32 * (5 + SX)) k_conv_halo(const __grid_consta
   tc::fence_after();
   const uint32_t tmem = tslot;
   bool ok = true;
-  if (warp == 4) {
+  if (warp == NEPI) {
     if (lane == 0) {
       // producer
       long long wq = 0;
@@ -278,11 +280,11 @@ __global__ void __launch_bounds__(32 * (5 + SX)) k_conv_halo(const __grid_consta
       }
     }
     __syncwarp();
-  } else if (warp >= 5) {
+  } else if (warp > NEPI) {
     if (lane == 0) {
       // MMA issuer of subtile sx.  Descriptors are linear in the start
       // address (field = address / 16): base descriptors plus offsets.
-      const int sx = warp - 5;
+      const int sx = warp - NEPI - 1;
       const uint32_t idesc = tc::idesc_bf16(TM, N);
       const uint64_t ad0 = tc::sdesc(tc::smem_u32(halo), SLAB, TXH * 16) + (uint64_t)(8 * sx);
       const uint64_t bd0 = tc::sdesc(tc::smem_u32(wst), 128, cu * 16);
@@ -325,8 +327,11 @@ __global__ void __launch_bounds__(32 * (5 + SX)) k_conv_halo(const __grid_consta
     }
     __syncwarp();
   } else {
-    // epilogue warps 0-3
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    // epilogue warps
+    const int quarter = warp & 3, half = warp >> 2;
+    const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
+    const int sx0 = SX >= 2 ? half : 0, sxs = SX >= 2 ? 2 : 1;
+    const int nlo = SX >= 2 ? 0 : half * (N / 2), nhi = SX >= 2 ? N : (half + 1) * (N / 2);
     int it = 0;
     for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, it++) {
       const int as = it & 1;
@@ -334,18 +339,18 @@ __global__ void __launch_bounds__(32 * (5 + SX)) k_conv_halo(const __grid_consta
       if (!got) { ok = false; break; }
       tc::fence_after();
       const int b = tile / per_img, r = tile - b * per_img;
-      const int y = (r / a.tiles_x) * TY + 4 * warp + (lane >> 3);
+      const int y = (r / a.tiles_x) * TY + 4 * quarter + (lane >> 3);
       const int x0 = (r % a.tiles_x) * 8 * SX;
-      for (int sx = 0; sx < SX; sx++) {
+      for (int sx = sx0; sx < SX; sx += sxs) {
         const int x = x0 + 8 * sx + (lane & 7);
-        int n0 = 0;
-        for (; n0 + 32 <= N; n0 += 32) {
+        int n0 = nlo;
+        for (; n0 + 32 <= nhi; n0 += 32) {
           float v[32];
           tc::tmem_ld32(trow + as * acc_cols + sx * N + n0, v);
 #pragma unroll
           for (int q = 0; q < 4; q++) epilogue8(a.e, s_bias, a.g, b, y, x, n0 + 8 * q, v + 8 * q);
         }
-        for (; n0 < N; n0 += 8) {
+        for (; n0 < nhi; n0 += 8) {
           float v[8];
           tc::tmem_ld8(trow + as * acc_cols + sx * N + n0, v);
           epilogue8(a.e, s_bias, a.g, b, y, x, n0, v);
@@ -872,7 +877,7 @@ int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int
     const dim3 grid(std::min(a.ntiles, net->nsm * net->cps));
     auto fn = halo_kernel(c.sx, c.kin / 16);
     if (!fn) return cfail(PQG_ERR_UNSUPPORTED, "no convolution kernel for this channel count");
-    fn<<<grid, 32 * (5 + c.sx), c.smem, st>>>(m, a);
+    fn<<<grid, 32 * (NEPI + 1 + c.sx), c.smem, st>>>(m, a);
   } else {
     GatherArgs a;
     a.in = in;

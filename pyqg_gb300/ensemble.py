@@ -58,6 +58,18 @@ def _member_constants(kind, kw):
     return nz, nx, np.ascontiguousarray(a), g["kk"], g["ll"], filtr, Ubg, Qy, float(rek)
 
 
+def shard_members(n, rank, world):
+    """Member indices of `rank` when n independent members are spread over
+    `world` GPUs (contiguous blocks, sizes differing by at most one); the
+    members need no exchange, so a multi-GPU ensemble is one Ensemble per
+    rank over its shard."""
+    if not 0 <= rank < world:
+        raise ValueError("rank out of range")
+    base, extra = divmod(n, world)
+    lo = rank * base + min(rank, extra)
+    return list(range(lo, lo + base + (1 if rank < extra else 0)))
+
+
 class EnsembleGroup:
     """B members of one shape, advanced by the batched CUDA step."""
 
