@@ -53,11 +53,16 @@ def _truncate_physical(q, nc):
 
 def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None):
     """Adam on standardised tensors X, Y (N, C, ny, nx); returns the mean
-    loss of every epoch."""
+    loss of every epoch.  A network without normalisation layers can
+    collapse at lr 1e-3 (all ReLUs dead: the loss jumps back to the variance
+    of the target); the best parameters are kept, and after an epoch whose
+    loss exceeds 1.5 times the best (or reaches 0.99) they are restored and
+    the learning rate is halved."""
     import torch
     g = torch.Generator(device="cpu").manual_seed(seed)
     n = X.shape[0] - X.shape[0] % batch
     hist = []
+    best, best_p = float("inf"), None
     for ep in range(epochs):
         perm = torch.randperm(X.shape[0], generator=g)[:n].to(X.device)
         tot = 0.0
@@ -66,7 +71,16 @@ def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None):
             tot += net.train_step(X[idx].contiguous(), Y[idx].contiguous(), lr=lr)
         hist.append(tot / (n // batch))
         if log:
-            log("epoch %d loss %.4f" % (ep, hist[-1]))
+            log("epoch %d loss %.4f lr %.2e" % (ep, hist[-1], lr))
+        if hist[-1] < best:
+            best, best_p = hist[-1], net.params
+        elif best_p is not None and (hist[-1] > 1.5 * best or hist[-1] >= 0.99):
+            net.params = best_p
+            lr *= 0.5
+            if log:
+                log("  restored the best parameters (loss %.4f), lr -> %.2e" % (best, lr))
+    if best_p is not None:
+        net.params = best_p
     return hist
 
 
@@ -107,7 +121,7 @@ def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30
         net.forward(Xs[i:j].contiguous(), pred[i:j])
     val = float(((pred - Ys[:n_val]) ** 2).mean() / (Ys[:n_val] ** 2).mean())
     report["training"] = dict(seconds=time.time() - t1, loss_first=hist[0], loss_last=hist[-1],
-                              validation_relative_mse=val)
+                              loss_best=min(hist), validation_relative_mse=val)
     log("training: loss %.4f -> %.4f, validation relative MSE %.3f" % (hist[0], hist[-1], val))
     param = CNNParameterization(net, (qm, qs, sm, ss))
 

@@ -77,8 +77,9 @@ def run(members=8, spinup_years=5.0, years=2.0, sample_every=240, seed0=2000, lo
                        samples=cnt, seed0=seed0),
         "ten_step_rel_l2_q": err10,
         "ke_spectrum": dict(max_rel_diff_energy_containing=float(rel[energetic].max()),
-                            mean_rel_diff_all=float(rel.mean()),
-                            total_ke_ratio=float(s32.sum() / s64.sum())),
+                            mean_rel_diff_energy_containing=float(rel[energetic].mean()),
+                            total_ke_ratio=float(s32.sum() / s64.sum()),
+                            bins_energy_containing=int(energetic.sum())),
         "eddy_pv_flux": dict(fp64=[float(x) for x in f64], fp32=[float(x) for x in f32],
                              rel_diff=[float(abs(x - y) / abs(y)) for x, y in zip(f32, f64)]),
         "seconds": time.time() - t0,
