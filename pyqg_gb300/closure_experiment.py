@@ -85,7 +85,7 @@ def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None):
 
 
 def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30, batch=64, lr=1e-3,
-        eval_years=3.0, spectra_every=240, seed0=2000, log=print):
+        eval_years=3.0, spectra_every=240, seed0=2000, scales=(1.0, 0.5), log=print):
     import torch
     import pyqg_gb300 as P
     from .closure import CNNParameterization, ConvNet
@@ -93,7 +93,8 @@ def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30
     t0 = time.time()
     report = {"config": dict(nruns=nruns, spinup_years=spinup_years, sample_years=sample_years,
                              sample_every_steps=sample_every, epochs=epochs, batch=batch, lr=lr,
-                             eval_years=eval_years, seed0=seed0, dt_fine=dt_f, dt_coarse=dt_c)}
+                             eval_years=eval_years, seed0=seed0, dt_fine=dt_f, dt_coarse=dt_c,
+                             closure_scales=list(scales))}
     spin = int(round(spinup_years * YEAR / dt_f))
     nsnap = max(1, int(round(sample_years * YEAR / dt_f / sample_every)))
     X, Y, ens_f = generate_training_data(nruns=nruns, nx_fine=256, nx_coarse=64, dt=dt_f, spinup_steps=spin,
@@ -123,37 +124,59 @@ def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30
     report["training"] = dict(seconds=time.time() - t1, loss_first=hist[0], loss_last=hist[-1],
                               loss_best=min(hist), validation_relative_mse=val)
     log("training: loss %.4f -> %.4f, validation relative MSE %.3f" % (hist[0], hist[-1], val))
-    param = CNNParameterization(net, (qm, qs, sm, ss))
+    CNNParameterization(net, (qm, qs, sm, ss))
+    params = net.params
 
     # ---- online comparison from the coarse-grained final fine states -----
+    # one closure ensemble per amplitude (the forcing times `scale`), each
+    # with its own copy of the network
     nm = nruns
     qf = ens_f.groups[0].get_q()
     q0c = [_truncate_physical(qf[j], 64) for j in range(nm)]
     coarse_members = [("qg", dict(nx=64, dt=dt_c, **PHYSICS)) for _ in range(nm)]
-    ens_cl = P.Ensemble(coarse_members, precision="fp32")
-    ens_cl.set_q(q0c)
-    ens_cl.set_closure(net)
+    runs = [("fine", ens_f, 2)]
+    closure_names = []
+    nets = []
+    for sc in scales:
+        nt = ConvNet(max_batch=max(batch, nruns), seed=seed0)
+        nt.params = params
+        CNNParameterization(nt, (qm, qs, sm * sc, ss * sc))
+        e = P.Ensemble(coarse_members, precision="fp32")
+        e.set_q(q0c)
+        e.set_closure(nt)
+        name = "closure" if sc == 1.0 else "closure_x%g" % sc
+        closure_names.append(name)
+        nets.append(nt)
+        runs.append((name, e, 1))
     ens_nc = P.Ensemble(coarse_members, precision="fp32")
     ens_nc.set_q(q0c)
+    runs.append(("no_closure", ens_nc, 1))
     m_f = P.QGModel(nx=256, dt=dt_f, **PHYSICS, **QUIET)
     m_c = P.QGModel(nx=64, dt=dt_c, **PHYSICS, **QUIET)
     n_c = int(round(eval_years * YEAR / dt_c))
     chunk = spectra_every
-    spec = {"fine": 0.0, "closure": 0.0, "no_closure": 0.0}
+    spec = {name: 0.0 for name, _, _ in runs}
     count = 0
-    wall = {"fine": 0.0, "closure": 0.0, "no_closure": 0.0}
+    wall = {name: 0.0 for name, _, _ in runs}
+    blowup = {}
     done = 0
     while done < n_c:
         c = min(chunk, n_c - done)
-        for name, ens, nsteps in (("fine", ens_f, 2 * c), ("closure", ens_cl, c), ("no_closure", ens_nc, c)):
+        for name, ens, mult in runs:
             torch.cuda.synchronize()
             ts = time.perf_counter()
-            ens.step(nsteps)
+            ens.step(mult * c)
             torch.cuda.synchronize()
             wall[name] += time.perf_counter() - ts
         done += c
+        for name, ens, _ in runs:
+            if name not in blowup:
+                ke_ = ens.energy()[0]
+                if not all(np.all(np.isfinite(k)) for k in ke_):
+                    blowup[name] = done * dt_c / YEAR
         if done * dt_c >= 0.5 * eval_years * YEAR:      # second half: statistics
-            for name, ens, model in (("fine", ens_f, m_f), ("closure", ens_cl, m_c), ("no_closure", ens_nc, m_c)):
+            for name, ens, _ in runs:
+                model = m_f if name == "fine" else m_c
                 qs_ = ens.groups[0].get_q()
                 s_ = 0.0
                 for j in range(nm):
@@ -172,7 +195,7 @@ def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30
     unfiltered = (kc[:nres] + dkr / 2) <= k_filter
     energetic = sf[:nres] >= 0.1 * sf[:nres].max()
     out = {}
-    for name in ("closure", "no_closure"):
+    for name in closure_names + ["no_closure"]:
         sc = spec[name] / count
         n = min(nres, len(sf))
         rel = np.abs(sc[:n] - sf[:n]) / np.maximum(np.abs(sf[:n]), 1e-300)
@@ -184,14 +207,14 @@ def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30
                                mean_rel_error=float(np.nanmean(rel[mask])) if finite else None,
                                bins=int(mask.sum()))
         out[name] = dict(bands=band, total_ke_ratio=float(sc[:n].sum() / sf[:n].sum()) if finite else None,
-                         finite=finite)
+                         finite=finite, blew_up_after_years=blowup.get(name))
     sim_years = n_c * dt_c / YEAR
     thr = {name: nm * sim_years / (wall[name] / 3600.0) for name in wall}
     report["online"] = dict(members=nm, years=sim_years, spectra_samples=count, ke_spectrum=out,
                             sim_years_per_hour=thr, k_resolved=[float(x) for x in kc[:nres]],
                             spectrum_fine=[float(x) for x in sf[:nres]],
-                            spectrum_closure=[float(x) for x in (spec["closure"] / count)[:nres]],
-                            spectrum_no_closure=[float(x) for x in (spec["no_closure"] / count)[:nres]])
+                            spectra={name: [float(x) for x in (spec[name] / count)[:nres]]
+                                     for name in closure_names + ["no_closure"]})
     report["seconds"] = time.time() - t0
     return report
 
@@ -204,10 +227,12 @@ def main(argv=None):
     ap.add_argument("--sample-every", type=int, default=48)
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--eval-years", type=float, default=3.0)
+    ap.add_argument("--scales", default="1.0,0.5", help="closure amplitudes to evaluate online")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     rep = run(nruns=a.nruns, spinup_years=a.spinup_years, sample_years=a.sample_years,
-              sample_every=a.sample_every, epochs=a.epochs, eval_years=a.eval_years)
+              sample_every=a.sample_every, epochs=a.epochs, eval_years=a.eval_years,
+              scales=tuple(float(x) for x in a.scales.split(",")))
     txt = json.dumps(rep)
     print(txt)
     if a.out:
