@@ -785,10 +785,11 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
   c.nchunk = (NTAP * kin + KC - 1) / KC;
   if (c.halo) {
     // One persistent CTA per SM.  Prefer wide tiles (one MMA issuer per 8
-    // columns), then two halo buffers, then resident weights; otherwise the
-    // deepest weight ring (at least 4 stages) within about 224 KiB of shared
-    // memory.  Two accumulators of SX N columns must fit in TMEM (512).
-    // PQG_CNN_SX caps the width (tuning).
+    // columns: more independent MMA streams measured faster than deeper
+    // weight rings, also for N = 64), then two halo buffers, then resident
+    // weights; otherwise the deepest weight ring (at least 4 stages) within
+    // about 224 KiB of shared memory.  Two accumulators of SX N columns must
+    // fit in TMEM (512).  PQG_CNN_SX caps the width (tuning).
     const size_t budget = 224 * 1024;
     int cap = 4;
     if (const char* e = getenv("PQG_CNN_SX")) cap = std::max(1, atoi(e));
