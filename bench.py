@@ -464,14 +464,11 @@ def closure_throughput(args, plain_value):
     return res
 
 
-def ensemble_throughput(args):
-    """Config-3 workload: 1024 FP32 members of uneven size (614 x nx=64,
-    307 x nx=128, 103 x nx=256; 20 % three-layer), beta and rek drawn per
-    member, autotuned launch shapes, groups on concurrent branches and
-    steady-state stretches replayed as CUDA graphs."""
-    import torch
+def config3_ensemble(rng):
+    """The config-3 members (614 x nx=64, 307 x nx=128, 103 x nx=256; 20 %
+    three-layer; beta and rek drawn per member) as an FP32 Ensemble with
+    seeded initial PV."""
     import pyqg_gb300 as P
-    rng = np.random.default_rng(1234)
     members = []
     for nx, cnt in ((64, 614), (128, 307), (256, 103)):
         dt = 3600.0 if nx == 256 else 7200.0
@@ -486,6 +483,16 @@ def ensemble_throughput(args):
     ens = P.Ensemble(members, precision="fp32")
     qs = [1e-7 * rng.standard_normal((3 if k == "layered" else 2, kw["nx"], kw["nx"])) for k, kw in members]
     ens.set_q(qs)
+    return ens, members
+
+
+def ensemble_throughput(args):
+    """Config-3 workload: 1024 FP32 members of uneven size, autotuned launch
+    shapes, groups on concurrent branches and steady-state stretches
+    replayed as CUDA graphs."""
+    import torch
+    rng = np.random.default_rng(1234)
+    ens, members = config3_ensemble(rng)
     ens.step(4)
     ens.autotune()
     stream = torch.cuda.current_stream()
@@ -519,6 +526,16 @@ def profile_case(args):
         m = P.QGModel(nx=args.nx, dt=3600.0, **C2, **QUIET)
         m.q = 1e-7 * np.random.default_rng(0).standard_normal((2, args.nx, args.nx))
         m._step_fused(args.profile_step)
+    if args.profile_ensemble:
+        ens, _ = config3_ensemble(np.random.default_rng(1234))
+        ens.step(4)
+        ens.autotune()
+        torch.cuda.synchronize()
+        # the steps a profiler should see: ncu --nvtx --nvtx-include "ensemble_steps/"
+        torch.cuda.nvtx.range_push("ensemble_steps")
+        ens.step(args.profile_ensemble)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     if args.profile_cnn:
         from pyqg_gb300.closure import ConvNet
         net = ConvNet(max_batch=args.profile_cnn, seed=0)
@@ -548,8 +565,10 @@ def main():
                     help="only run N fused nx=256 steps (a small case for profilers) and exit")
     ap.add_argument("--profile-cnn", type=int, default=0, metavar="B",
                     help="only run two closure-network forwards of a batch of B and exit")
+    ap.add_argument("--profile-ensemble", type=int, default=0, metavar="N",
+                    help="only run N steps of the config-3 FP32 ensemble and exit")
     args = ap.parse_args()
-    if args.profile_step or args.profile_cnn:
+    if args.profile_step or args.profile_cnn or args.profile_ensemble:
         profile_case(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -17,15 +17,22 @@
 // halo a copy of the opposite edge), written by every producer, so that no
 // consumer wraps indices.  Master weights are FP32 w[co][tap][ci].
 //
-// Two convolution kernels:
-//  * k_conv_halo (input channels a multiple of 16): a CTA computes a tile of
-//    16 rows x 8 SX columns.  TMA loads the input tile with its halo once into
+// Three convolution kernels:
+//  * k_conv_rows (64 input channels, at most 32 outputs): a tile is
+//    two full image rows, so every A operand window is aligned, and the five
+//    horizontal taps are folded into the MMA's N dimension (N = 5 x 32 for 32
+//    output channels); the epilogue sums the horizontally shifted columns.
+//    It replaces five N = 32 MMAs, bound by reading the A operand from shared
+//    memory, with one N = 160 MMA bound by the tensor pipe, at the price of
+//    a five times wider epilogue.
+//  * k_conv_halo (input channels a multiple of 16, the other layers): a CTA
+//    computes a tile of 16 rows x 8 SX columns.  TMA loads the input tile with its halo once into
 //    shared memory as one slab per 8 channels (pixel-major, 16 bytes per
 //    pixel); the A operand of tap (dy, dx) is then a shifted descriptor over
 //    the same slabs (core matrix = 8 consecutive pixels of a row, next
 //    8-pixel group = next image row).  The per-tap weight blocks stream
 //    through a bulk-copy ring of `nst` stages (all 25 taps resident when
-//    they fit); one thread issues the MMAs.
+//    they fit); one thread per 8-column subtile issues its MMAs.
 //  * k_conv_gather (few input channels, e.g. the 2-channel input layer):
 //    threads gather a K-chunk of 64 (tap, channel) pairs per pixel.
 // The weight gradient gathers (tap, channel) x pixel tiles (k_wgrad) and
@@ -377,6 +384,339 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
 }
 
 // ---------------------------------------------------------------------------
+// row-tile convolution (image width 64, input channels 16, 32, 64 or 128),
+// persistent and warp-specialised, one CTA per SM, 18 warps.
+//
+// A tile is two full image rows (M = 128 pixels, row-major), so the A
+// operand of vertical offset dy is the aligned 128-pixel window starting at
+// halo row dy: no operand window is shifted by a pixel.  The five horizontal
+// taps are folded into N instead:
+//     D[p][dx * CO + co] = sum_{dy, ci} in[p + (dy - 2, 0)][ci] w[co][dy][dx][ci]
+//     out[y][x][co]      = sum_dx D[(y, (x + dx - 2) mod 64)][dx * CO + co]
+// so one MMA of N = 5 CO (160 for 32 output channels) per (dy, 16 input
+// channels) replaces five MMAs of N = CO, and the horizontal sum (periodic
+// within the row) is done by the epilogue with warp shuffles.
+//   warps 0-15  epilogue.  Warp w reads TMEM lanes 32 (w % 4) .., i.e. 32
+//               pixels of one row half, and the 8-channel group w / 4 of the
+//               output unit; w and w ^ 1 hold the two halves of a row and
+//               swap, through shared memory, the few values that the lane
+//               rotations of the horizontal sum carry across their edges.
+//   warp 16     producer (one lane): TMA halo tiles (6 rows x 64 pixels x
+//               up to 64 channels per channel unit) into `nh` buffers and
+//               weight blocks (output unit, channel unit, dy) into a ring of
+//               `nst` stages, or once when all blocks are resident.
+//   warp 17     MMA issuer (one lane).
+// Output channels are processed in units of CO (<= 32) into a ring of `nacc`
+// TMEM accumulators of Nu = pad16(5 CO) columns.  Inputs of 128 channels are
+// pipelined in two units of 64 channels, reloaded for every output unit.
+// ---------------------------------------------------------------------------
+constexpr int RT = 2;                  // image rows per tile
+constexpr int RH = RT + 2 * PAD;       // halo rows
+constexpr int RW = 64;                 // image width
+constexpr int RSLAB = RH * RW * 16;    // bytes per 8 channels of a halo tile
+constexpr int RMAXST = 40;             // weight stages / resident blocks
+constexpr int RNACC = 4;               // accumulator slots at most
+constexpr int REPI = 16;               // epilogue warps (four per TMEM lane quarter)
+constexpr int RMAXH = 4;               // halo buffers at most
+constexpr uint64_t kLimit = 1000000000ull;   // bound of every pipeline wait (ns)
+
+struct RowArgs {
+  const bf16* wpk;       // blocks ((o * CH + h) * 5 + dy) of Nu x cu, K-major core matrices
+  int cout;              // real output channels
+  int CO;                // output channels per unit (<= 32)
+  int nuo;               // output units
+  int Nu;                // pad16(5 CO)
+  int nacc;              // accumulator slots (nacc Nu <= 512)
+  int nst;               // weight stages (nuo CH 5: resident)
+  int nh;                // halo buffers (1 .. RMAXH)
+  int ntiles;            // batch * H / 2
+  uint32_t hint;         // producer / issuer waits: sleep after every miss (ns)
+  uint32_t ehint;        // epilogue waits: the same
+  Img g;
+  Epi e;
+  int* err;
+};
+
+// x8 TMEM load without the wait (the caller waits once for several loads)
+__device__ __forceinline__ void tmem_ld8_nw(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+// the wait, with 8 loaded registers passed through it
+__device__ __forceinline__ void tmem_wait8(uint32_t* r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])
+               :: "memory");
+}
+// no instruction: keeps the uses of r after the preceding wait
+__device__ __forceinline__ void reg_after8(uint32_t* r) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])
+               :: "memory");
+}
+
+// v[dx][c] = s[dx K + c] for the K (< 8) channels of a small output unit
+template <int K>
+__device__ __forceinline__ void spread_small(const uint32_t* s, uint32_t (*v)[8]) {
+#pragma unroll
+  for (int dx = 0; dx < 5; dx++)
+#pragma unroll
+    for (int c = 0; c < 8; c++) v[dx][c] = c < K ? s[dx * K + c] : 0u;
+}
+
+template <int KU, int CH, bool SMALL>
+__global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_constant__ CUtensorMap tmap, RowArgs a) {
+  constexpr int cu = 16 * KU, groups = 2 * KU;   // channels and 8-channel slabs per channel unit
+  constexpr uint32_t hbytes = (uint32_t)groups * RSLAB;
+  extern __shared__ __align__(1024) unsigned char csm[];
+  __shared__ __align__(8) uint64_t hfull[RMAXH], hempty[RMAXH], afull[RNACC], aempty[RNACC], wfull[RMAXST],
+      wempty[RMAXST];
+  __shared__ __align__(8) uint64_t xbar[2][REPI / 2];
+  __shared__ __align__(16) float xbuf[2][REPI][4][16];   // edge values swapped between the two warps of a row
+  __shared__ uint32_t tslot;
+  __shared__ int s_fail;
+  __shared__ float s_bias[128];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int Nu = a.Nu, CO = a.CO, NUO = a.nuo, NST = a.nst, NH = a.nh, NACC = a.nacc;
+  const int nblk = NUO * CH * 5;
+  const bool resident = NST >= nblk;
+  unsigned char* halo = csm;                        // NH buffers
+  unsigned char* wst = csm + (size_t)NH * hbytes;   // NST stages
+  const uint32_t wbytes = (uint32_t)Nu * cu * 2;
+  const int per_img = a.g.H / RT;
+  const uint32_t ncols = tmem_cols(NACC * Nu);
+  if (warp == 0) tc::tmem_alloc(&tslot, ncols);
+  if (tid == 0) {
+    for (int i = 0; i < RMAXH; i++) {
+      tc::mbar_init(&hfull[i], 1);
+      tc::mbar_init(&hempty[i], 1);
+    }
+    for (int i = 0; i < 2; i++)
+      for (int p = 0; p < REPI / 2; p++) tc::mbar_init(&xbar[i][p], 64);
+    for (int i = 0; i < NACC; i++) {
+      tc::mbar_init(&afull[i], 1);
+      tc::mbar_init(&aempty[i], 32 * REPI);
+    }
+    for (int s = 0; s < (resident ? nblk : NST); s++) {
+      tc::mbar_init(&wfull[s], 1);
+      tc::mbar_init(&wempty[s], 1);
+    }
+    tc::mbar_fence_init();
+    s_fail = 0;
+  }
+  for (int i = tid; i < 128; i += blockDim.x) s_bias[i] = (a.e.bias && i < a.e.cout) ? a.e.bias[i] : 0.f;
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  bool ok = true;
+  if (warp == REPI) {
+    if (lane == 0) {
+      // producer
+      long long wq = 0;
+      int hq = 0;
+      bool first = true;
+      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+        const int b = tile / per_img, y0 = (tile - b * per_img) * RT;
+        if (resident && first) {
+          for (int blk = 0; blk < nblk; blk++) {
+            tc::mbar_expect_tx(&wfull[blk], wbytes);
+            tc::bulk_load(wst + (size_t)blk * wbytes, a.wpk + (size_t)blk * Nu * cu, wbytes, &wfull[blk]);
+          }
+        }
+        first = false;
+        for (int o = 0; o < NUO && ok; o++) {
+          for (int h = 0; h < CH && ok; h++) {
+            if (CH > 1 || o == 0) {
+              const int hs = hq % NH;
+              if (hq >= NH) ok = tc::mbar_wait(&hempty[hs], ((hq - NH) / NH) & 1, kLimit, a.hint);
+              if (!ok) break;
+              tc::mbar_expect_tx(&hfull[hs], hbytes);
+              // padded rows y0 .. y0 + 5 hold image rows y0 - 2 .. y0 + 3
+              for (int gq = 0; gq < groups; gq++)
+                tc::tma_load_4d(halo + (size_t)hs * hbytes + (size_t)gq * RSLAB, &tmap, cu * h + 8 * gq, PAD, y0, b,
+                                &hfull[hs]);
+              hq++;
+            }
+            if (!resident) {
+              for (int dy = 0; dy < 5 && ok; dy++, wq++) {
+                const int ws = (int)(wq % NST);
+                if (wq >= NST) ok = tc::mbar_wait(&wempty[ws], (int)(((wq - NST) / NST) & 1), kLimit, a.hint);
+                if (!ok) break;
+                tc::mbar_expect_tx(&wfull[ws], wbytes);
+                tc::bulk_load(wst + (size_t)ws * wbytes, a.wpk + (size_t)((o * CH + h) * 5 + dy) * Nu * cu, wbytes,
+                              &wfull[ws]);
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == REPI + 1) {
+    if (lane == 0) {
+      // MMA issuer.  Descriptors are linear in the start address (field =
+      // address / 16): base descriptors plus offsets.
+      const uint32_t idesc = tc::idesc_bf16(TM, Nu);
+      const uint64_t ad0 = tc::sdesc(tc::smem_u32(halo), RSLAB, 128);
+      const uint64_t bd0 = tc::sdesc(tc::smem_u32(wst), 128, cu * 16);
+      long long wq = 0;
+      int hq = 0, aq = 0, hs = 0;
+      bool first = true;
+      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+        for (int o = 0; o < NUO && ok; o++, aq++) {
+          const int slot = aq % NACC;
+          if (aq >= NACC) ok = tc::mbar_wait(&aempty[slot], ((aq - NACC) / NACC) & 1, kLimit, a.hint);
+          if (!ok) break;
+          tc::fence_after();
+          const uint32_t acc = tmem + slot * Nu;
+          for (int h = 0; h < CH && ok; h++) {
+            if (CH > 1 || o == 0) {
+              hs = hq % NH;
+              ok = tc::mbar_wait(&hfull[hs], (hq / NH) & 1, kLimit, a.hint);
+              if (!ok) break;
+              tc::fence_after();
+            }
+            const uint64_t adh = ad0 + (uint64_t)hs * (hbytes >> 4);
+            for (int dy = 0; dy < 5 && ok; dy++) {
+              const int blk = (o * CH + h) * 5 + dy;
+              const int ws = resident ? blk : (int)(wq % NST);
+              if (!resident || first) {
+                ok = tc::mbar_wait(&wfull[ws], resident ? 0 : (int)((wq / NST) & 1), kLimit, a.hint);
+                if (!ok) break;
+                tc::fence_after();
+              }
+              const uint64_t at = adh + (uint64_t)(dy * RW);   // dy rows of 64 pixels x 16 bytes
+              const uint64_t bt = bd0 + (uint64_t)ws * (wbytes >> 4);
+#pragma unroll
+              for (int kk = 0; kk < KU; kk++)
+                tc::mma_bf16(acc, at + (uint64_t)(kk * (2 * RSLAB / 16)), bt + (uint64_t)(16 * kk), idesc,
+                             (dy | kk | h) ? 1u : 0u);
+              if (!resident) {
+                tc::mma_commit(&wempty[ws]);
+                wq++;
+              }
+            }
+            if (!ok) break;
+            if (CH > 1 || o == NUO - 1) {
+              tc::mma_commit(&hempty[hs]);
+              hq++;
+            }
+          }
+          if (!ok) break;
+          tc::mma_commit(&afull[slot]);
+        }
+        first = false;
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue warps: `quarter` is the TMEM lane quarter (32 pixels of one
+    // row half), `grp` the 8-channel group of the output unit
+    const int quarter = warp & 3, grp = warp >> 2, pair = warp >> 1;
+    const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
+    const int edge = lane < 2 ? lane : (lane >= 30 ? lane - 28 : -1);
+    const bool active = SMALL ? grp == 0 : 8 * grp < CO;
+    int aq = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+      const int b = tile / per_img;
+      const int y = (tile - b * per_img) * RT + (quarter >> 1), x = 32 * (quarter & 1) + lane;
+      for (int o = 0; o < NUO; o++, aq++) {
+        const int slot = aq % NACC, par = aq & 1;
+        const bool got = __all_sync(0xffffffffu, tc::mbar_wait(&afull[slot], (aq / NACC) & 1, kLimit, a.ehint));
+        if (!got) { ok = false; break; }
+        tc::fence_after();
+        const uint32_t tacc = trow + slot * Nu;
+        uint32_t v[5][8];   // v[dx][c]: horizontal tap dx, channel 8 grp + c of this pixel
+        if (active) {
+          if (SMALL) {
+            uint32_t s16[16];   // CO <= 3: the 5 CO used columns lie in the first 16
+            tmem_ld8_nw(tacc, s16);
+            tmem_ld8_nw(tacc + 8, s16 + 8);
+            tmem_wait8(s16);
+            reg_after8(s16 + 8);
+            if (CO == 1) spread_small<1>(s16, v);
+            else if (CO == 2) spread_small<2>(s16, v);
+            else spread_small<3>(s16, v);
+          } else {
+#pragma unroll
+            for (int dx = 0; dx < 5; dx++) tmem_ld8_nw(tacc + dx * CO + 8 * grp, v[dx]);
+            tmem_wait8(v[0]);
+#pragma unroll
+            for (int dx = 1; dx < 5; dx++) reg_after8(v[dx]);
+          }
+        }
+        tc::fence_before();
+        tc::mbar_arrive(&aempty[slot]);   // the accumulator is in registers
+        // The horizontal sum rotates the 32 lanes by dx - 2.  The values
+        // that the rotation wraps around (tap 0 of lanes 30-31, tap 1 of lane
+        // 31, tap 3 of lane 0, tap 4 of lanes 0-1) are used only by pixels of
+        // the partner warp (the other half of the row, periodically): swap
+        // them with the partner first, then every rotation is exact.
+        if (active && edge >= 0) {
+          float4* xb = reinterpret_cast<float4*>(xbuf[par][warp][edge]);
+          uint32_t sa[8], sb[8];
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            sa[c] = lane >= 30 ? v[0][c] : (lane == 0 ? v[3][c] : v[4][c]);
+            sb[c] = lane == 31 ? v[1][c] : v[4][c];
+          }
+          xb[0] = make_float4(__uint_as_float(sa[0]), __uint_as_float(sa[1]), __uint_as_float(sa[2]), __uint_as_float(sa[3]));
+          xb[1] = make_float4(__uint_as_float(sa[4]), __uint_as_float(sa[5]), __uint_as_float(sa[6]), __uint_as_float(sa[7]));
+          xb[2] = make_float4(__uint_as_float(sb[0]), __uint_as_float(sb[1]), __uint_as_float(sb[2]), __uint_as_float(sb[3]));
+          xb[3] = make_float4(__uint_as_float(sb[4]), __uint_as_float(sb[5]), __uint_as_float(sb[6]), __uint_as_float(sb[7]));
+        }
+        tc::mbar_arrive(&xbar[par][pair]);
+        const bool swapped =
+            __all_sync(0xffffffffu, tc::mbar_wait(&xbar[par][pair], (aq >> 1) & 1, kLimit, a.ehint));
+        if (!swapped) { ok = false; break; }
+        if (!active) continue;
+        if (edge >= 0) {
+          const float4* pb = reinterpret_cast<const float4*>(xbuf[par][warp ^ 1][edge]);
+          const float4 q0 = pb[0], q1 = pb[1], q2 = pb[2], q3 = pb[3];
+          const uint32_t ra[8] = {__float_as_uint(q0.x), __float_as_uint(q0.y), __float_as_uint(q0.z), __float_as_uint(q0.w),
+                                  __float_as_uint(q1.x), __float_as_uint(q1.y), __float_as_uint(q1.z), __float_as_uint(q1.w)};
+          const uint32_t rb[8] = {__float_as_uint(q2.x), __float_as_uint(q2.y), __float_as_uint(q2.z), __float_as_uint(q2.w),
+                                  __float_as_uint(q3.x), __float_as_uint(q3.y), __float_as_uint(q3.z), __float_as_uint(q3.w)};
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            if (lane >= 30) v[0][c] = ra[c];
+            if (lane == 31) v[1][c] = rb[c];
+            if (lane == 0) { v[3][c] = ra[c]; v[4][c] = rb[c]; }
+            if (lane == 1) v[4][c] = ra[c];
+          }
+        }
+        float out[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          const float t0 = __shfl_sync(0xffffffffu, __uint_as_float(v[0][c]), (lane + 30) & 31);
+          const float t1 = __shfl_sync(0xffffffffu, __uint_as_float(v[1][c]), (lane + 31) & 31);
+          const float t3 = __shfl_sync(0xffffffffu, __uint_as_float(v[3][c]), (lane + 1) & 31);
+          const float t4 = __shfl_sync(0xffffffffu, __uint_as_float(v[4][c]), (lane + 2) & 31);
+          out[c] = __uint_as_float(v[2][c]) + t0 + t1 + t3 + t4;
+        }
+        epilogue8(a.e, s_bias, a.g, b, y, x, o * CO + 8 * grp, out);
+      }
+    }
+  }
+  if (!ok) s_fail = 1;
+  __syncthreads();
+  if (s_fail) {
+    if (tid == 0) {
+      atomicExch(a.err, 1);
+      // give copies and MMAs still in flight a bounded time before TMEM is freed
+      tc::mbar_wait(&hfull[0], 0, 10000000ull);
+      tc::mbar_wait(&hfull[1], 0, 10000000ull);
+    }
+    __syncthreads();
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
 // gather convolution (few input channels): K chunks of 64 (tap, channel)
 // ---------------------------------------------------------------------------
 struct GatherArgs {
@@ -676,6 +1016,33 @@ __global__ void k_pack_taps(const float* __restrict__ w, int cin, int cout, int 
   }
 }
 
+// packing for the row-tile kernel: blocks ((o * CH + h) * 5 + dy) of Nu x cu,
+// row n = dx * CO + co of output unit o (rows 5 CO .. Nu - 1 zero), cu = kpad
+// / CH channels along K (channels beyond the real K channels zero)
+__global__ void k_pack_rows(const float* __restrict__ w, int cin, int cout, int transpose, bf16* __restrict__ out,
+                            int CO, int Nu, int kpad, int CH, int nuo) {
+  const int kin = transpose ? cout : cin;
+  const int nreal = transpose ? cin : cout;
+  const int cu = kpad / CH;
+  const size_t total = (size_t)nuo * CH * 5 * Nu * cu;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int blk = (int)(i / ((size_t)Nu * cu));
+    const int rem = (int)(i - (size_t)blk * Nu * cu);
+    const int n = rem / cu, cl = rem - n * cu;
+    const int dy = blk % 5, oh = blk / 5, h = oh % CH, o = oh / CH;
+    const int ch = h * cu + cl;
+    float v = 0.f;
+    if (n < 5 * CO) {
+      const int dx = n / CO, co = o * CO + n % CO, tap = dy * 5 + dx;
+      if (co < nreal && ch < kin) {
+        if (!transpose) v = w[((size_t)co * NTAP + tap) * cin + ch];
+        else v = w[((size_t)ch * NTAP + (NTAP - 1 - tap)) * cin + co];
+      }
+    }
+    out[(size_t)blk * Nu * cu + tc::kmajor_off(n, cl, cu) / 2] = __float2bfloat16_rn(v);
+  }
+}
+
 // MSE loss of y (NCHW FP32) against t; gradient 2 (y - t) / count as padded
 // NHWC BF16
 __global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, bf16* __restrict__ g, int B, int C,
@@ -730,9 +1097,13 @@ struct ConvPlan {
   int kin = 0, nout = 0;   // channels along K (input) and real output channels
   int N = 0;               // pad16(nout)
   bool halo = false;       // halo kernel (kin % 16 == 0) or gather kernel
+  bool rows = false;       // row-tile kernel (width 64; replaces the halo kernel)
   int sx = 0;              // halo kernel tile width / 8
-  int nst = 0;             // halo kernel weight stages
-  int nh = 0;              // halo kernel halo buffers
+  int nst = 0;             // halo / row-tile kernel weight stages
+  int nh = 0;              // halo / row-tile kernel halo buffers
+  int co = 0, nuo = 0;     // row-tile kernel: output channels per unit, units
+  int nun = 0, nacc = 0;   // row-tile kernel: MMA N per unit, accumulator slots
+  int ch = 1;              // row-tile kernel: input channel units
   int nchunk = 0;          // gather kernel K chunks
   bf16* w = nullptr;
   size_t smem = 0;
@@ -753,6 +1124,8 @@ struct pqg_cnn {
   int nl = 0, H = 0, W = 0, maxB = 0;
   int nsm = 1;                // SM count
   int cps = 1;                // persistent CTAs per SM
+  uint32_t hint = 0;          // row-tile kernel: producer / issuer waits sleep this long after a miss (ns)
+  uint32_t ehint = 0;         // row-tile kernel: epilogue waits, the same
   Img g{};
   std::vector<CnnLayer> L;
   size_t nparams = 0;
@@ -777,12 +1150,56 @@ size_t gather_smem(int N) { return 2 * (size_t)CHUNK_A + 2 * (size_t)N * KC * 2;
 
 size_t halo_bytes(int sx, int kin) { return (size_t)(kin / 8) * (8 * sx + 2 * PAD) * TYH * 16; }
 
+size_t rows_halo_bytes(int cu) { return (size_t)(cu / 8) * RSLAB; }
+
+// row-tile kernel plan: false if the layer does not take it.  By default
+// only 64 input channels and one output unit of at most 32 channels: there
+// the MMA saving outweighs the longer epilogue (5 TMEM columns and 4 lane
+// shuffles per output instead of 1 column), measured 277 us against 432 us
+// for the 64 -> 32 layer at batch 512; for 16 or 32 input channels, or
+// several output units, the epilogue's instruction issue bounds the kernel
+// above the halo kernel's time.  PQG_CNN_ROWS=2 takes every layer that fits,
+// PQG_CNN_ROWS=0 none.
+bool plan_rows(ConvPlan& c, int W, int kin, int nout) {
+  int mode = 1;
+  if (const char* e = getenv("PQG_CNN_ROWS")) mode = atoi(e);
+  if (mode <= 0) return false;
+  if (W != RW || !(kin == 16 || kin == 32 || kin == 64 || kin == 128)) return false;
+  if (!((nout <= 32 && (nout % 8 == 0 || nout <= 3)) || nout % 32 == 0)) return false;
+  if (mode == 1 && !(kin == 64 && nout <= 32)) return false;
+  c.ch = kin > 64 ? 2 : 1;
+  const int cu = kin / c.ch;
+  c.co = std::min(nout, 32);
+  c.nuo = (nout + c.co - 1) / c.co;
+  c.nun = pad16(5 * c.co);
+  c.nacc = std::min(RNACC, 512 / c.nun);
+  if (const char* e = getenv("PQG_CNN_NACC")) c.nacc = std::max(1, std::min(c.nacc, atoi(e)));
+  const int nblk = c.nuo * c.ch * 5;
+  const size_t wb = (size_t)c.nun * cu * 2, hb = rows_halo_bytes(cu);
+  const size_t budget = 212 * 1024;   // + the kernel's static shared memory (10 KB)
+  c.nst = 0;
+  int nhmax = RMAXH;
+  if (const char* e = getenv("PQG_CNN_NH")) nhmax = std::max(1, std::min(RMAXH, atoi(e)));
+  for (int nh = nhmax; nh >= 1; nh--) {
+    if (nblk <= RMAXST && nh * hb + nblk * wb <= budget) { c.nh = nh; c.nst = nblk; break; }
+    const int nst = (int)std::min<size_t>(std::min(RMAXST, nblk - 1), (budget - nh * hb) / wb);
+    if (nh * hb < budget && nst >= 4) { c.nh = nh; c.nst = nst; break; }
+  }
+  if (!c.nst) return false;
+  c.smem = c.nh * hb + (size_t)c.nst * wb;
+  // more than half of TMEM per CTA: keep one CTA per SM through shared memory
+  if (c.nacc * c.nun > 256) c.smem = std::max<size_t>(c.smem, 120 * 1024);
+  c.rows = true;
+  return true;
+}
+
 void plan_conv(ConvPlan& c, int W, int kin, int nout) {
   c.kin = kin;
   c.nout = nout;
   c.N = pad16(nout);
-  c.halo = kin == 16 || kin == 32 || kin == 64 || kin == 128;
   c.nchunk = (NTAP * kin + KC - 1) / KC;
+  if (plan_rows(c, W, kin, nout)) return;
+  c.halo = kin == 16 || kin == 32 || kin == 64 || kin == 128;
   if (c.halo) {
     // One persistent CTA per SM.  Prefer wide tiles (one MMA issuer per 8
     // columns: more independent MMA streams measured faster than deeper
@@ -817,10 +1234,12 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
 }
 
 size_t plan_weight_elems(const ConvPlan& c) {
+  if (c.rows) return (size_t)c.nuo * 5 * c.nun * c.kin;
   return c.halo ? (size_t)NTAP * c.N * c.kin : (size_t)c.nchunk * c.N * KC;
 }
 
-int encode_map(CUtensorMap* m, const bf16* buf, int C, const pqg_cnn* net, int sx) {
+// 4-D map of a padded NHWC buffer; boxes of 8 channels x bw pixels x bh rows
+int encode_map(CUtensorMap* m, const bf16* buf, int C, const pqg_cnn* net, int bw, int bh) {
   if (!g_encode) {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -831,7 +1250,7 @@ int encode_map(CUtensorMap* m, const bf16* buf, int C, const pqg_cnn* net, int s
   }
   cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)net->g.Wp, (cuuint64_t)net->g.Hp, (cuuint64_t)net->maxB};
   cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)net->g.Wp * C * 2, (cuuint64_t)net->g.Hp * net->g.Wp * C * 2};
-  cuuint32_t box[4] = {8, (cuuint32_t)(8 * sx + 2 * PAD), (cuuint32_t)TYH, 1};
+  cuuint32_t box[4] = {8, (cuuint32_t)bw, (cuuint32_t)bh, 1};
   cuuint32_t es[4] = {1, 1, 1, 1};
   CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(buf), dims, strides, box, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -857,12 +1276,51 @@ HaloFn halo_kernel(int sx, int ks) {
   return nullptr;
 }
 
+typedef void (*RowFn)(const __grid_constant__ CUtensorMap, RowArgs);
+RowFn rows_kernel(int kin, bool small) {
+#define RK(KU, CH)                                                     \
+  return small ? k_conv_rows<KU, CH, true> : k_conv_rows<KU, CH, false>;
+  switch (kin) {
+    case 16: RK(1, 1)
+    case 32: RK(2, 1)
+    case 64: RK(4, 1)
+    case 128: RK(4, 2)
+    default: return nullptr;
+  }
+#undef RK
+}
+
 int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int batch, const Epi& e,
                 cudaStream_t st) {
   const ConvPlan& c = dgrad ? l.bwd : l.fwd;
-  if (c.halo) {
+  if (c.rows) {
+    const bool small = c.co < 8;
+    if (small && e.mode != 1) return cfail(PQG_ERR_UNSUPPORTED, "fewer than 8 channels only at the network output");
     CUtensorMap m;
-    int rc = encode_map(&m, in, c.kin, net, c.sx);
+    int rc = encode_map(&m, in, c.kin, net, RW, RH);
+    if (rc) return rc;
+    RowArgs a;
+    a.wpk = c.w;
+    a.cout = c.nout;
+    a.CO = c.co;
+    a.nuo = c.nuo;
+    a.Nu = c.nun;
+    a.nacc = c.nacc;
+    a.nst = c.nst;
+    a.nh = c.nh;
+    a.ntiles = batch * (net->H / RT);
+    a.hint = net->hint;
+    a.ehint = net->ehint;
+    a.g = net->g;
+    a.e = e;
+    a.err = net->err;
+    const dim3 grid(std::min(a.ntiles, net->nsm * net->cps));
+    auto fn = rows_kernel(c.kin, small);
+    if (!fn) return cfail(PQG_ERR_UNSUPPORTED, "no convolution kernel for this channel count");
+    fn<<<grid, 32 * (REPI + 2), c.smem, st>>>(m, a);
+  } else if (c.halo) {
+    CUtensorMap m;
+    int rc = encode_map(&m, in, c.kin, net, 8 * c.sx + 2 * PAD, TYH);
     if (rc) return rc;
     HaloArgs a;
     a.cin = c.kin;
@@ -937,6 +1395,9 @@ int set_attrs() {
   for (int sx : {1, 2, 4})
     for (int ks : {1, 2, 4, 8})
       CCUDA(cudaFuncSetAttribute(halo_kernel(sx, ks), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  for (int kin : {16, 32, 64, 128})
+    for (bool small : {false, true})
+      CCUDA(cudaFuncSetAttribute(rows_kernel(kin, small), cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 12288));
   CCUDA(cudaFuncSetAttribute(k_conv_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_wgrad<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   CCUDA(cudaFuncSetAttribute(k_wgrad<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -951,7 +1412,10 @@ int repack(pqg_cnn* net, cudaStream_t st) {
   for (auto& l : net->L) {
     for (int d = 0; d < 2; d++) {
       const ConvPlan& c = d ? l.bwd : l.fwd;
-      if (c.halo)
+      if (c.rows)
+        k_pack_rows<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w, c.co,
+                                                                    c.nun, c.kin, c.ch, c.nuo);
+      else if (c.halo)
         k_pack_taps<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w, c.N,
                                                                    c.kin, c.kin > 64 ? c.kin / 64 : 1);
       else
@@ -1025,6 +1489,8 @@ PQG_API int pqg_cnn_create(pqg_cnn** out, int nlayers, const int* channels, int 
     cudaDeviceGetAttribute(&net->nsm, cudaDevAttrMultiProcessorCount, dev);
     if (net->nsm < 1) net->nsm = 1;
     if (const char* e = getenv("PQG_CNN_CPS")) net->cps = std::max(1, std::min(4, atoi(e)));
+    if (const char* e = getenv("PQG_CNN_HINT")) net->hint = (uint32_t)std::max(0, atoi(e));
+    if (const char* e = getenv("PQG_CNN_EHINT")) net->ehint = (uint32_t)std::max(0, atoi(e));
   }
   size_t off = 0;
   for (int i = 0; i < nlayers; i++) {

@@ -91,30 +91,24 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 }
 
 // wait for the phase of the given parity to complete, for at most
-// `limit_ns` nanoseconds of wall time; false on timeout
-// (`sleep_ns` > 0: a suspend-time hint, so that a waiter that is not on the
-// critical path sleeps until the phase completes instead of spinning)
+// `limit_ns` nanoseconds of wall time; false on timeout.  `backoff_ns` > 0
+// sleeps that long after every miss, so that waiting warps leave the issue
+// slots (and the barrier word) to the warps doing the work.
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint64_t limit_ns = 1000000000ull,
-                                          uint32_t sleep_ns = 0) {
+                                          uint32_t backoff_ns = 0) {
   const uint32_t a = smem_u32(mbar);
   uint64_t t0 = 0;
   for (uint32_t it = 0;; it++) {
     uint32_t done;
-    if (sleep_ns)
-      asm volatile(
-          "{\n\t.reg .pred p;\n\t"
-          "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-          "selp.u32 %0, 1, 0, p;\n\t}"
-          : "=r"(done) : "r"(a), "r"(parity), "r"(sleep_ns) : "memory");
-    else
-      asm volatile(
-          "{\n\t.reg .pred p;\n\t"
-          "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-          "selp.u32 %0, 1, 0, p;\n\t}"
-          : "=r"(done) : "r"(a), "r"(parity) : "memory");
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done) : "r"(a), "r"(parity) : "memory");
     if (done) return true;
     if (it == 0) t0 = globaltimer_ns();
     else if (globaltimer_ns() - t0 > limit_ns) return false;
+    if (backoff_ns) __nanosleep(backoff_ns);
   }
 }
 

@@ -271,3 +271,39 @@ def test_default_net_learns():
     losses = [net.train_step(x, t, lr=1e-3) for _ in range(150)]
     assert np.all(np.isfinite(losses))
     assert losses[-1] < 0.3 * losses[0], (losses[0], losses[-1])
+
+
+@pytest.mark.parametrize("channels,batch", [((2, 24, 40, 32, 2), 3), ((2, 128, 64, 32, 32, 2), 40)])
+def test_row_tile_and_halo_kernels_agree(channels, batch, monkeypatch):
+    """The row-tile kernel (horizontal taps folded into N) on every layer it
+    takes, the default choice, and the halo kernel (one MMA per tap) on
+    every layer, on the same network: forward and gradients."""
+    import torch
+    from pyqg_gb300.closure import ConvNet
+    nets = []
+    for rows in ("2", "1", "0"):
+        monkeypatch.setenv("PQG_CNN_ROWS", rows)
+        nets.append(ConvNet(channels, max_batch=batch, seed=13))
+    p = _he_params(nets[0], 13)
+    rng = np.random.default_rng(13)
+    p += (0.02 * rng.standard_normal(p.shape)).astype(np.float32)
+    for n in nets:
+        n.params = p
+    x = torch.from_numpy(rng.standard_normal((batch, 2, 64, 64)).astype(np.float32)).cuda()
+    t = torch.from_numpy(rng.standard_normal((batch, 2, 64, 64)).astype(np.float32)).cuda()
+    ys = [n.forward(x).cpu().numpy() for n in nets]
+    ref = _torch_net(channels, p, nets[0].layer_slices(), x).cpu().numpy()
+    for y in ys:
+        assert rel_l2(y, ref) < 1e-2
+        for b in range(batch):
+            assert rel_l2(y[b], ref[b]) < 2e-2, b
+    for y in ys[1:]:
+        assert rel_l2(ys[0], y) < 1e-2
+    gs = []
+    for n in nets:
+        n.backward(x, t)
+        gs.append(n.grads)
+    for ws, shape, bs in nets[0].layer_slices():
+        for g in gs[1:]:
+            assert rel_l2(gs[0][ws], g[ws]) < 2e-2
+            assert rel_l2(gs[0][bs], g[bs]) < 2e-2
