@@ -175,6 +175,61 @@ __device__ __forceinline__ void epilogue8(const Epi& e, const float* bias, const
   }
 }
 
+// mode 0 (bias + ReLU -> padded NHWC BF16) without per-call address work:
+// the store addresses of an output pixel and of its periodic halo copies,
+// computed once per pixel
+struct PixOut {
+  bf16* p0;              // the pixel
+  bf16* p1;              // x halo copy (h1)
+  bf16* p2;              // y halo copy (h2)
+  bf16* p3;              // corner copy (h1 && h2)
+  bool h1, h2;
+};
+
+__device__ __forceinline__ PixOut pix_out(bf16* buf, int C, const Img& g, int b, int y, int x) {
+  // padded coordinates of the pixel and of its periodic image (the same
+  // when it has none)
+  const int y0 = y + PAD, x0 = x + PAD;
+  const int y1 = y < PAD ? y0 + g.H : (y >= g.H - PAD ? y0 - g.H : y0);
+  const int x1 = x < PAD ? x0 + g.W : (x >= g.W - PAD ? x0 - g.W : x0);
+  PixOut o;
+  o.h1 = x1 != x0;
+  o.h2 = y1 != y0;
+  o.p0 = buf + g.pix(b, y0, x0) * C;
+  o.p1 = buf + g.pix(b, y0, x1) * C;
+  o.p2 = buf + g.pix(b, y1, x0) * C;
+  o.p3 = buf + g.pix(b, y1, x1) * C;
+  return o;
+}
+
+// K (multiple of 8) accumulator columns n0.. of one pixel: + bias, ReLU,
+// BF16 (round to nearest even, as epilogue8), 16-byte stores; `bias` is a
+// 16-byte aligned shared-memory vector
+template <int K>
+__device__ __forceinline__ void relu_store(const PixOut& o, const float* bias, int n0, const float* v) {
+  uint32_t w[K / 2];
+#pragma unroll
+  for (int i = 0; i < K / 4; i++) {
+    const float4 bb = *reinterpret_cast<const float4*>(bias + n0 + 4 * i);
+    float t0 = v[4 * i] + bb.x, t1 = v[4 * i + 1] + bb.y, t2 = v[4 * i + 2] + bb.z, t3 = v[4 * i + 3] + bb.w;
+    t0 = t0 > 0.f ? t0 : 0.f;
+    t1 = t1 > 0.f ? t1 : 0.f;
+    t2 = t2 > 0.f ? t2 : 0.f;
+    t3 = t3 > 0.f ? t3 : 0.f;
+    const __nv_bfloat162 h01 = __floats2bfloat162_rn(t0, t1), h23 = __floats2bfloat162_rn(t2, t3);
+    w[2 * i] = *reinterpret_cast<const uint32_t*>(&h01);
+    w[2 * i + 1] = *reinterpret_cast<const uint32_t*>(&h23);
+  }
+#pragma unroll
+  for (int q = 0; q < K / 8; q++) {
+    const uint4 u = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    *reinterpret_cast<uint4*>(o.p0 + n0 + 8 * q) = u;
+    if (o.h1) *reinterpret_cast<uint4*>(o.p1 + n0 + 8 * q) = u;
+    if (o.h2) *reinterpret_cast<uint4*>(o.p2 + n0 + 8 * q) = u;
+    if (o.h1 && o.h2) *reinterpret_cast<uint4*>(o.p3 + n0 + 8 * q) = u;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // halo-tile convolution (input channels 16, 32, 64 or 128), persistent and
 // warp-specialised, one CTA per SM, 9 + SX warps:
@@ -220,7 +275,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
   __shared__ __align__(8) uint64_t hfull[2], hempty[2], afull[2], aempty[2], wfull[MAXST], wempty[MAXST];
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
-  __shared__ float s_bias[256];
+  __shared__ __align__(16) float s_bias[256];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int N = a.N, NST = a.nst, NH = a.nh;
   const bool resident = NST >= NTAP * CH;
@@ -350,17 +405,25 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
       const int x0 = (r % a.tiles_x) * 8 * SX;
       for (int sx = sx0; sx < SX; sx += sxs) {
         const int x = x0 + 8 * sx + (lane & 7);
+        const bool fast = a.e.mode == 0;
+        PixOut po{};
+        if (fast) po = pix_out(a.e.out_bf, a.e.cout, a.g, b, y, x);
         int n0 = nlo;
         for (; n0 + 32 <= nhi; n0 += 32) {
           float v[32];
           tc::tmem_ld32(trow + as * acc_cols + sx * N + n0, v);
+          if (fast && n0 + 32 <= a.e.cout) {
+            relu_store<32>(po, s_bias, n0, v);
+          } else {
 #pragma unroll
-          for (int q = 0; q < 4; q++) epilogue8(a.e, s_bias, a.g, b, y, x, n0 + 8 * q, v + 8 * q);
+            for (int q = 0; q < 4; q++) epilogue8(a.e, s_bias, a.g, b, y, x, n0 + 8 * q, v + 8 * q);
+          }
         }
         for (; n0 < nhi; n0 += 8) {
           float v[8];
           tc::tmem_ld8(trow + as * acc_cols + sx * N + n0, v);
-          epilogue8(a.e, s_bias, a.g, b, y, x, n0, v);
+          if (fast && n0 + 8 <= a.e.cout) relu_store<8>(po, s_bias, n0, v);
+          else epilogue8(a.e, s_bias, a.g, b, y, x, n0, v);
         }
       }
       tc::fence_before();
@@ -476,7 +539,7 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
   __shared__ __align__(16) float xbuf[2][REPI][4][16];   // edge values swapped between the two warps of a row
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
-  __shared__ float s_bias[128];
+  __shared__ __align__(16) float s_bias[128];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int Nu = a.Nu, CO = a.CO, NUO = a.nuo, NST = a.nst, NH = a.nh, NACC = a.nacc;
   const int nblk = NUO * CH * 5;
@@ -622,6 +685,9 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
     for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
       const int b = tile / per_img;
       const int y = (tile - b * per_img) * RT + (quarter >> 1), x = 32 * (quarter & 1) + lane;
+      const bool fast = a.e.mode == 0;
+      PixOut po{};
+      if (fast) po = pix_out(a.e.out_bf, a.e.cout, a.g, b, y, x);
       for (int o = 0; o < NUO; o++, aq++) {
         const int slot = aq % NACC, par = aq & 1;
         const bool got = __all_sync(0xffffffffu, tc::mbar_wait(&afull[slot], (aq / NACC) & 1, kLimit, a.ehint));
@@ -696,7 +762,9 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
           const float t4 = __shfl_sync(0xffffffffu, __uint_as_float(v[4][c]), (lane + 2) & 31);
           out[c] = __uint_as_float(v[2][c]) + t0 + t1 + t3 + t4;
         }
-        epilogue8(a.e, s_bias, a.g, b, y, x, o * CO + 8 * grp, out);
+        const int n0 = o * CO + 8 * grp;
+        if (fast && n0 + 8 <= a.e.cout) relu_store<8>(po, s_bias, n0, out);
+        else epilogue8(a.e, s_bias, a.g, b, y, x, n0, out);
       }
     }
   }
