@@ -1294,6 +1294,21 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
         if (score > best) { best = score; c.sx = sx; c.nh = nh; c.nst = nst; }
       }
     }
+    // tuning override for one layer shape: PQG_CNN_HALO_<kin>_<nout>=<sx>,<nh>
+    char key[64];
+    snprintf(key, sizeof key, "PQG_CNN_HALO_%d_%d", kin, nout);
+    if (const char* e = getenv(key)) {
+      int sx = 0, nh = 0;
+      if (sscanf(e, "%d,%d", &sx, &nh) == 2 && (sx == 1 || sx == 2 || sx == 4) && (nh == 1 || nh == 2) &&
+          W % (8 * sx) == 0 && 2 * sx * c.N <= 512) {
+        const size_t h = (size_t)nh * halo_bytes(sx, cu);
+        if (h + (size_t)NTAP * nu * wb <= budget) {
+          best = 1; c.sx = sx; c.nh = nh; c.nst = NTAP * nu;
+        } else if (h < budget && (budget - h) / wb >= 4) {
+          best = 1; c.sx = sx; c.nh = nh; c.nst = (int)std::min<size_t>(NTAP * nu - 1, (budget - h) / wb);
+        }
+      }
+    }
     if (best < 0) c.halo = false;
   }
   const int nu = kin > 64 ? kin / 64 : 1;
