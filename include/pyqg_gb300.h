@@ -191,9 +191,18 @@ int pqg_ens_step(pqg_ens *ens, int nsteps, void *stream);
 int pqg_ens_step_many(pqg_ens **ens, int count, int nsteps, void *stream);
 /* autotuner: times the row kernel over (rows per CTA, threads) and the
  * fused column kernel over (columns per CTA, threads) on the ensemble's own
- * state, keeps the fastest and restores the state; out (may be NULL) gets
- * {rows per CTA, row threads, row ms, columns per CTA, column threads,
- * column ms}.  Synchronizes `stream`. */
+ * state, keeps the fastest, then, for square grids of 16 to 64 points (FP64:
+ * up to 32) and at most 4 layers, times four whole steps of the per-member
+ * kernel (one CTA per member, the member's mixed planes resident in shared
+ * memory; 128 or 256 threads) against four steps of the row and column
+ * kernels and keeps the faster schedule.  The state is restored.  out (may
+ * be NULL, else 10 values) gets {rows per CTA, row threads, row ms, columns
+ * per CTA, column threads, column ms, per-member kernel chosen (0 / 1), its
+ * threads, its ms for four steps, the two-kernel ms for four steps}.
+ * Without the autotuner the row and column kernels run; PQG_ENS_FUSED=1 /
+ * 0 forces the per-member kernel on / off where the shape allows it.
+ * Ensembles with a closure always use the row and column kernels.
+ * Synchronizes `stream`. */
 int pqg_ens_autotune(pqg_ens *ens, double *out, void *stream);
 /* FP64 sums per (member, layer): ke = 0.5 sum |kappa ph|^2 / M^2 and
  * enstrophy 0.5 sum |qh|^2 / M^2 over the full spectral plane (host out) */

@@ -366,6 +366,181 @@ __global__ void e_col_fwd(EGeo g, const V* scratch, V* qh, const V* __restrict__
   }
 }
 
+// ---------------------------------------------------------------------------
+// whole model steps of one member per CTA, for square grids small enough
+// that the member's mixed planes U, V, Q (3 nz x nk x N values) fit in
+// shared memory: the prologue, n steps and the epilogue of the two-kernel
+// path (e_col_invert; e_row_adv + e_col_fused per step; e_row_c2r) in one
+// launch, with the same transforms and pointwise operations in the same
+// order, so the results are identical.  The mixed planes never leave shared
+// memory; qh and the AB3 history stay in global memory (each value is read
+// and written by the same thread every step).
+// Shared: [tw (N)] [planes (f, z) at (f nz + z) nk N, k-major] [row buffers
+// U, V, Q: rb x M each].
+// ---------------------------------------------------------------------------
+constexpr int kMemberMaxZ = 4;
+
+template <class S>
+struct AbCoef { S c1[3], c2[3], c3[3]; };   // per start-up level 0, 1, 2
+
+// The phases are separate (not inlined) functions.  At most 512 threads
+// (FP32: 128 registers a thread) or 256 (FP64).
+template <class V, int LOGN>
+__device__ __noinline__ void member_prologue(const EGeo& g, const EConsts<typename Sc<V>::T>& c, const V* qh, V* P,
+                                             const V* tw, int b) {
+  typedef typename Sc<V>::T S;
+  constexpr int N = 1 << LOGN, nk = N / 2 + 1;
+  const int nz = g.nz;
+  const size_t plane = (size_t)N * nk;
+  for (int t = threadIdx.x; t < nz * nk * N; t += blockDim.x) {
+    const int z = t / (nk * N), ck = t - z * nk * N;
+    const int k = ck / N, l = ck - k * N;
+    V p = mk((S)0, (S)0);
+    for (int z1 = 0; z1 < nz; z1++)
+      p = g_ph_acc(p, c.a[((size_t)z * nz + z1) * plane + ck], qh[sidx(b, z1, l, k, nz, N, nk)]);
+    P[(size_t)z * plane + ck] = g_uh(c.ll[l], p);
+    P[(size_t)(nz + z) * plane + ck] = g_vh(c.kk[k], p);
+  }
+  __syncthreads();
+  Pow2Fft<N, 1, true, V>::run(P, N, 2 * nz * nk, tw, 1);
+}
+
+// rows of one model step (e_row_adv); `first`: q from its physical field
+template <class V, int LOGN>
+__device__ __noinline__ void member_rows(const EGeo& g, const EConsts<typename Sc<V>::T>& c,
+                                         const typename Sc<V>::T* q, V* P, V* bU, const V* tw,
+                                         typename Sc<V>::T scale, int b, bool first, int rb) {
+  typedef typename Sc<V>::T S;
+  constexpr int N = 1 << LOGN, M = N / 2, nk = M + 1, half = M / 2 + 1;
+  const int nz = g.nz;
+  const size_t plane = (size_t)N * nk;
+  V* bV = bU + rb * M;
+  V* bQ = bV + rb * M;
+  for (int r0 = 0; r0 < nz * N; r0 += rb) {
+    const int z = r0 / N, y0 = r0 - z * N;
+    for (int t = threadIdx.x; t < 3 * rb * half; t += blockDim.x) {
+      const int rr = t % rb, rest = t / rb;
+      const int k = rest % half, f = rest / half;
+      V* buf = (f == 0 ? bU : (f == 1 ? bV : bQ)) + rr * M;
+      if (f < 2 || !first) {
+        c2r_pre_s(P + (size_t)(f * nz + z) * plane + y0 + rr, N, buf, M, k, tw);
+      } else {
+        const V* row = reinterpret_cast<const V*>(q + (((size_t)b * nz + z) * N + y0 + rr) * N);
+        if (k < M - k) buf[k] = row[k];
+        if (k < M - k && M - 1 - k != k) buf[M - 1 - k] = row[M - 1 - k];
+      }
+    }
+    __syncthreads();
+    Pow2Fft<M, 1, true, V>::run(bU, M, (first ? 2 : 3) * rb, tw, 2);
+    const S ub = c.Ubg[b * nz + z];
+    for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+      const V u = cscale(bU[t], scale), v = cscale(bV[t], scale);
+      V qq = bQ[t];
+      if (!first) qq = cscale(qq, scale);
+      bU[t] = mk(smul(sadd(u.x, ub), qq.x), smul(sadd(u.y, ub), qq.y));
+      bV[t] = mk(smul(v.x, qq.x), smul(v.y, qq.y));
+    }
+    __syncthreads();
+    Pow2Fft<M, 1, false, V>::run(bU, M, 2 * rb, tw, 2);
+    for (int t = threadIdx.x; t < 2 * rb * half; t += blockDim.x) {
+      const int rr = t % rb, rest = t / rb;
+      const int k = rest % half, f = rest / half;
+      r2c_post_s((f == 0 ? bU : bV) + rr * M, P + (size_t)(f * nz + z) * plane + y0 + rr, N, M, k, tw);
+    }
+    __syncthreads();
+  }
+}
+
+// columns of one model step (e_col_fused without forcing): the new qh of
+// every layer goes to plane Q first (global qh still holds the old values
+// the other layers' inversions read), then to qh and through the inversion
+// to U and V
+template <class V, int LOGN>
+__device__ __noinline__ void member_cols(const EGeo& g, const EConsts<typename Sc<V>::T>& c, V* qh, const V* dqp,
+                                         V* dqpp, V* P, const V* tw, int b, typename Sc<V>::T c1,
+                                         typename Sc<V>::T c2, typename Sc<V>::T c3) {
+  typedef typename Sc<V>::T S;
+  constexpr int N = 1 << LOGN, nk = N / 2 + 1;
+  const int nz = g.nz;
+  const size_t plane = (size_t)N * nk;
+  const S rek = c.rek[b];
+  Pow2Fft<N, 1, false, V>::run(P, N, 2 * nz * nk, tw, 1);
+  for (int t = threadIdx.x; t < nz * nk * N; t += blockDim.x) {
+    const int z = t / (nk * N), ck = t - z * nk * N;
+    const int k = ck / N, l = ck - k * N;
+    V p = mk((S)0, (S)0);
+    for (int z1 = 0; z1 < nz; z1++)
+      p = g_ph_acc(p, c.a[((size_t)z * nz + z1) * plane + ck], qh[sidx(b, z1, l, k, nz, N, nk)]);
+    const S kQy = c.kQy[((size_t)b * nz + z) * nk + k];
+    V d = g_tendency(c.kk[k], c.ll[l], kQy, P[(size_t)z * plane + ck], P[(size_t)(nz + z) * plane + ck], p);
+    if (rek != (S)0 && z == nz - 1) d = g_friction(d, smul(rek, c.k2l2[ck]), p);
+    const size_t o = sidx(b, z, l, k, nz, N, nk);
+    P[(size_t)(2 * nz + z) * plane + ck] = g_ab(c.filtr[ck], qh[o], d, dqp[o], dqpp[o], c1, c2, c3);
+    dqpp[o] = d;   // the newest tendency takes the oldest one's buffer
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nz * nk * N; t += blockDim.x) {
+    const int z = t / (nk * N), ck = t - z * nk * N;
+    const int k = ck / N, l = ck - k * N;
+    qh[sidx(b, z, l, k, nz, N, nk)] = P[(size_t)(2 * nz + z) * plane + ck];
+    V p = mk((S)0, (S)0);
+    for (int z1 = 0; z1 < nz; z1++)
+      p = g_ph_acc(p, c.a[((size_t)z * nz + z1) * plane + ck], P[(size_t)(2 * nz + z1) * plane + ck]);
+    P[(size_t)z * plane + ck] = g_uh(c.ll[l], p);
+    P[(size_t)(nz + z) * plane + ck] = g_vh(c.kk[k], p);
+  }
+  __syncthreads();
+  Pow2Fft<N, 1, true, V>::run(P, N, 3 * nz * nk, tw, 1);
+}
+
+// physical q from mixed plane Q (e_row_c2r)
+template <class V, int LOGN>
+__device__ __noinline__ void member_epilogue(const EGeo& g, typename Sc<V>::T* q, const V* P, V* bQ, const V* tw,
+                                             typename Sc<V>::T scale, int b, int rb) {
+  constexpr int N = 1 << LOGN, M = N / 2, nk = M + 1, half = M / 2 + 1;
+  const int nz = g.nz;
+  const size_t plane = (size_t)N * nk;
+  for (int r0 = 0; r0 < nz * N; r0 += rb) {
+    const int z = r0 / N, y0 = r0 - z * N;
+    for (int t = threadIdx.x; t < rb * half; t += blockDim.x) {
+      const int rr = t % rb, k = t / rb;
+      c2r_pre_s(P + (size_t)(2 * nz + z) * plane + y0 + rr, N, bQ + rr * M, M, k, tw);
+    }
+    __syncthreads();
+    Pow2Fft<M, 1, true, V>::run(bQ, M, rb, tw, 2);
+    for (int t = threadIdx.x; t < rb * M; t += blockDim.x) {
+      const int rr = t / M, m = t - rr * M;
+      *reinterpret_cast<V*>(q + (((size_t)b * nz + z) * N + y0 + rr) * N + 2 * m) = cscale(bQ[t], scale);
+    }
+    __syncthreads();
+  }
+}
+
+template <class V, int LOGN>
+__global__ void __launch_bounds__(sizeof(V) == 8 ? 512 : 256) e_member_steps(EGeo g, EConsts<typename Sc<V>::T> c, V* qh, V* dqp,
+                                                      V* dqpp, typename Sc<V>::T* q, const V* __restrict__ tw_g,
+                                                      typename Sc<V>::T scale, AbCoef<typename Sc<V>::T> ab,
+                                                      int ablevel, int nsteps, int rb) {
+  constexpr int N = 1 << LOGN, nk = N / 2 + 1;
+  extern __shared__ __align__(16) unsigned char esm[];
+  const int b = blockIdx.x;
+  V* tw = reinterpret_cast<V*>(esm);
+  V* P = tw + N;
+  V* bU = P + 3 * (size_t)g.nz * N * nk;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw_g[i];
+  __syncthreads();
+  member_prologue<V, LOGN>(g, c, qh, P, tw, b);
+  for (int s = 0; s < nsteps; s++) {
+    const int lvl = min(ablevel + s, 2);
+    member_rows<V, LOGN>(g, c, q, P, bU, tw, scale, b, s == 0, rb);
+    member_cols<V, LOGN>(g, c, qh, dqp, dqpp, P, tw, b, ab.c1[lvl], ab.c2[lvl], ab.c3[lvl]);
+    V* tmp = dqp;
+    dqp = dqpp;
+    dqpp = tmp;
+  }
+  member_epilogue<V, LOGN>(g, q, P, bU + 2 * rb * (N / 2), tw, scale, b, rb);
+}
+
 // precision conversions between an FP64 staging buffer and the state
 template <class S>
 __global__ void e_from_f64(const double* src, S* dst, size_t n) {
@@ -443,6 +618,9 @@ struct pqg_ens {
   long long tc = 0;
   double t = 0.0, dt = 0.0;
   int T_row = 128, rb = 1, T_col = 128, C = 1;
+  bool fused = false;           // whole steps per CTA (e_member_steps; the autotuner's choice)
+  int T_mem = 256;              // threads of the per-member kernel
+  int rb_mem = 16;              // its rows per chunk of the row transforms
   int nfield = 3;               // mixed planes per member: U, V, Q (+ forcing F)
   long long version = 0;        // bumped when launch parameters change (graph cache key)
   pqg_cnn* net = nullptr;       // closure: forcing = net(q) every step
@@ -504,6 +682,16 @@ int lg2(int n) { int l = 0; while ((1 << l) < n) l++; return l; }
 template <class V>
 struct EK {
   typedef typename Sc<V>::T S;
+  typedef void (*Member)(EGeo, EConsts<S>, V*, V*, V*, S*, const V*, S, AbCoef<S>, int, int, int);
+  static Member member(int N) {
+    switch (lg2(N)) {
+      case 4: return e_member_steps<V, 4>;
+      case 5: return e_member_steps<V, 5>;
+      case 6: return member64();
+      default: return nullptr;
+    }
+  }
+  static Member member64();
   typedef void (*RowAdv)(EGeo, EConsts<S>, V*, const S*, const V*, S, int, S*);
   typedef void (*ColFused)(EGeo, EConsts<S>, V*, V*, const V*, V*, const V*, S, S, S, int, int);
   typedef void (*ColInv)(EGeo, EConsts<S>, V*, const V*, const V*, int);
@@ -653,8 +841,67 @@ int launch_closure(pqg_ens* e, cudaStream_t st) {
   return PQG_OK;
 }
 
+// nx = 64 members only in FP32 (FP64 planes do not fit in shared memory)
+template <>
+EK<float2>::Member EK<float2>::member64() { return e_member_steps<float2, 6>; }
+template <>
+EK<double2>::Member EK<double2>::member64() { return nullptr; }
+
+// per-member kernel: rows per chunk and shared memory; 0 when the group's
+// shape does not fit it (square, 16 <= nx <= 64, at most 4 layers, FP64
+// only up to nx = 32, shared memory within the 200 KB the kernels opt in to)
+int member_rb(const pqg_ens* e) { return std::min(e->ny, e->rb_mem); }
+size_t member_smem(const pqg_ens* e) {
+  if (e->nx != e->ny || e->nx < 16 || e->nx > 64 || e->nz > kMemberMaxZ || (e->prec == 8 && e->nx > 32)) return 0;
+  const size_t n = (size_t)e->nx + 3 * (size_t)e->nz * e->nk * e->ny + 3 * (size_t)member_rb(e) * e->M;
+  const size_t b = vsz(e) * n;
+  return b <= 200 * 1024 ? b : 0;
+}
+bool member_on(const pqg_ens* e) {
+  if (e->net || !member_smem(e)) return false;
+  if (const char* env = getenv("PQG_ENS_FUSED")) {   // 1: always, 0: never
+    if (env[0] == '1') return true;
+    if (env[0] == '0') return false;
+  }
+  return e->fused;
+}
+
+// nsteps model steps of every member, one CTA per member (launches of at
+// most 256 steps)
 template <class V>
-int step_impl(pqg_ens* e, int nsteps, cudaStream_t st) {
+int launch_member(pqg_ens* e, int nsteps, cudaStream_t st) {
+  typedef typename Sc<V>::T S;
+  AbCoef<S> ab;
+  const double dt = e->dt;
+  const double c1[3] = {dt, 1.5 * dt, 23. / 12. * dt}, c2[3] = {0.0, -0.5 * dt, -16. / 12. * dt},
+               c3[3] = {0.0, 0.0, 5. / 12. * dt};
+  for (int i = 0; i < 3; i++) {
+    ab.c1[i] = (S)c1[i];
+    ab.c2[i] = (S)c2[i];
+    ab.c3[i] = (S)c3[i];
+  }
+  const size_t smem = member_smem(e);
+  auto fn = EK<V>::member(e->nx);
+  if (!fn || !smem) return efail(PQG_ERR_UNSUPPORTED, "no per-member kernel for this shape");
+  for (int done = 0; done < nsteps;) {
+    const int n = std::min(256, nsteps - done);
+    fn<<<e->B, e->T_mem, smem, st>>>(egeo(e), econsts<V>(e), (V*)e->qh, (V*)e->dq[e->role_p],
+                                      (V*)e->dq[e->role_pp], (S*)e->q, (const V*)e->twy,
+                                      (S)(1.0 / ((double)e->nx * e->ny)), ab, e->ablevel, n, member_rb(e));
+    ECUDA(cudaGetLastError());
+    // the same bookkeeping as n launches of the column kernel
+    if (n & 1) std::swap(e->role_p, e->role_pp);
+    e->ablevel = std::min(2, e->ablevel + n);
+    e->tc += n;
+    for (int i = 0; i < n; i++) e->t += e->dt;
+    done += n;
+  }
+  return PQG_OK;
+}
+
+// the row and column kernels
+template <class V>
+int step_two(pqg_ens* e, int nsteps, cudaStream_t st) {
   int rc = launch_prologue<V>(e, st);
   for (int i = 0; i < nsteps && !rc; i++) {
     rc = launch_row_adv<V>(e, i == 0, st);
@@ -663,6 +910,11 @@ int step_impl(pqg_ens* e, int nsteps, cudaStream_t st) {
   }
   if (!rc) rc = launch_epilogue<V>(e, st);
   return rc;
+}
+
+template <class V>
+int step_impl(pqg_ens* e, int nsteps, cudaStream_t st) {
+  return member_on(e) ? launch_member<V>(e, nsteps, st) : step_two<V>(e, nsteps, st);
 }
 
 template <class V>
@@ -693,6 +945,8 @@ int set_attrs(pqg_ens* e) {
   ECUDA(cudaFuncSetAttribute(EK<V>::col_fused(e->ny), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   ECUDA(cudaFuncSetAttribute(EK<V>::col_inv(e->ny), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   ECUDA(cudaFuncSetAttribute(EK<V>::col_fwd(e->ny), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  if (member_smem(e))
+    ECUDA(cudaFuncSetAttribute(EK<V>::member(e->nx), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   return PQG_OK;
 }
 
@@ -1052,6 +1306,28 @@ int autotune_impl(pqg_ens* e, cudaStream_t st, double* out) {
   }
   e->C = bc;
   e->T_col = btc;
+  // whole steps: the per-member kernel (threads 128 .. 512) against the
+  // row and column kernels with the shapes just chosen
+  float t_two = 0.f, best_m = 0.f;
+  if (!rc && !e->net && member_smem(e)) {
+    t_two = time3([&]() { step_two<V>(e, 4, st); });
+    best_m = 1e30f;
+    int bt = e->T_mem, br = e->rb_mem;
+    for (int rbm : {8, 16, 32}) {
+      if (rbm > e->ny) continue;
+      e->rb_mem = rbm;
+      if (!member_smem(e)) continue;
+      for (int tm : {128, 256, 512}) {
+        if (tm > (e->prec == 4 ? 512 : 256)) continue;
+        e->T_mem = tm;
+        const float ms = time3([&]() { launch_member<V>(e, 4, st); });
+        if (ms < best_m) { best_m = ms; bt = tm; br = rbm; }
+      }
+    }
+    e->T_mem = bt;
+    e->rb_mem = br;
+    e->fused = best_m < t_two;
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   ECUDA(cudaMemcpyAsync(e->qh, sv, vb, cudaMemcpyDeviceToDevice, st));
@@ -1069,6 +1345,8 @@ int autotune_impl(pqg_ens* e, cudaStream_t st, double* out) {
   if (out) {
     out[0] = e->rb; out[1] = e->T_row; out[2] = best_r;
     out[3] = e->C; out[4] = e->T_col; out[5] = best_c;
+    out[6] = member_smem(e) && e->fused && !e->net ? 1.0 : 0.0; out[7] = e->T_mem;
+    out[8] = best_m; out[9] = t_two;
   }
   return rc;
 }

@@ -133,10 +133,12 @@ class EnsembleGroup:
     def autotune(self):
         """Pick the fastest row / column launch configuration on this
         group's state (the state is restored); returns the choice."""
-        out = np.zeros(6)
+        out = np.zeros(10)
         self._check(self._L.pqg_ens_autotune(self._h, out.ctypes.data, self._sp()))
         return dict(rows_per_cta=int(out[0]), row_threads=int(out[1]), row_ms=float(out[2]),
-                    cols_per_cta=int(out[3]), col_threads=int(out[4]), col_ms=float(out[5]))
+                    cols_per_cta=int(out[3]), col_threads=int(out[4]), col_ms=float(out[5]),
+                    member_kernel=bool(out[6]), member_threads=int(out[7]),
+                    member_ms_4_steps=float(out[8]), two_kernel_ms_4_steps=float(out[9]))
 
     def set_closure(self, net):
         """Attach a :class:`~pyqg_gb300.closure.ConvNet` (or None): every step

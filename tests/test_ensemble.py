@@ -146,3 +146,69 @@ def test_autotune_keeps_the_state_and_results():
     b.step(40)
     for i in range(3):
         np.testing.assert_array_equal(a.q(i), b.q(i))
+
+
+def test_large_members_up_to_nx512():
+    """Members of nx = 256 and 512 beside a small one: the FP64 form equals
+    the single-model FP64 step bit for bit, and the FP32 form stays within
+    FP32 rounding of it over a few steps."""
+    import pyqg_gb300 as P
+    rng = np.random.default_rng(5)
+    specs = [_qg(1.5e-11, 5.787e-7, nx=512, dt=1800.0), _qg(1.2e-11, 4.0e-7, nx=256, dt=3600.0),
+             _qg(1.5e-11, 5.787e-7, nx=64)]
+    q0 = [1e-7 * rng.standard_normal((2, kw["nx"], kw["nx"])) for _, kw in specs]
+    e64 = P.Ensemble(specs, precision="fp64")
+    e32 = P.Ensemble(specs, precision="fp32")
+    for e in (e64, e32):
+        e.set_q(q0)
+        e.step(6)
+    for i in (0, 1):
+        kw = specs[i][1]
+        m = P.QGModel(nx=kw["nx"], dt=kw["dt"], beta=kw["beta"], rek=kw["rek"], tmax=6 * kw["dt"], **QUIET)
+        m.engine = "fp64"
+        m.q = q0[i]
+        m.run()
+        np.testing.assert_array_equal(e64.q(i), m.q)
+        assert rel_l2(e32.q(i), m.q) < 1e-5
+
+
+def test_member_kernel_equals_row_and_column_kernels(monkeypatch):
+    """The per-member kernel (whole steps of one member per CTA, mixed planes
+    in shared memory) runs the same operations as the row and column
+    kernels: identical states, also through graph replay."""
+    import pyqg_gb300 as P
+    rng = np.random.default_rng(7)
+    lay = dict(nz=3, H=[500., 1000., 2500.], U=[0.05, 0.02, 0.0], V=[0., 0., 0.])
+    specs = [_qg(1.5e-11, 5.787e-7), _qg(2.0e-11, 3.0e-7), ("layered", dict(nx=64, dt=7200.0, **lay)),
+             _qg(1.1e-11, 6.0e-7, nx=32), _qg(1.5e-11, 5.787e-7, nx=16)]
+    q0 = [1e-7 * rng.standard_normal((3 if k == "layered" else 2, kw["nx"], kw["nx"])) for k, kw in specs]
+    out = []
+    for fused in ("0", "1"):
+        monkeypatch.setenv("PQG_ENS_FUSED", fused)
+        e = P.Ensemble(specs, precision="fp32")
+        e.set_q(q0)
+        e.step(3)          # start-up steps
+        e.step(37)         # graph replay of the steady state
+        out.append([e.q(i) for i in range(len(specs))])
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_member_kernel_fp64_equals_single_models(monkeypatch):
+    import pyqg_gb300 as P
+    monkeypatch.setenv("PQG_ENS_FUSED", "1")
+    rng = np.random.default_rng(8)
+    specs = [_qg(1.5e-11, 5.787e-7, nx=32), _qg(0.7e-11, 9.0e-7, nx=32)]
+    q0 = [1e-7 * rng.standard_normal((2, 32, 32)) for _ in specs]
+    ens = P.Ensemble(specs, precision="fp64")
+    ens.set_q(q0)
+    ens.step(30)
+    for i, (kind, kw) in enumerate(specs):
+        m = P.QGModel(nx=32, dt=7200.0, beta=kw["beta"], rek=kw["rek"], tmax=30 * 7200.0, **QUIET)
+        m.engine = "fp64"
+        m.q = q0[i]
+        m.run()
+        np.testing.assert_array_equal(ens.q(i), m.q)
+    monkeypatch.delenv("PQG_ENS_FUSED")
+    tuned = ens.autotune()
+    assert set(tuned[0]) >= {"member_kernel", "member_threads", "member_ms_4_steps"}
