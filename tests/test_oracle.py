@@ -121,3 +121,41 @@ def test_oracle_vs_live_reference_nx96():
         m._step_forward()
         o.step()
     np.testing.assert_array_equal(o.q, m.q)
+
+
+def test_reference_multithreaded_fft_variant_is_bit_identical():
+    """The CPU baseline's multithreaded-FFT variant of the compiled reference
+    kernel (its FFT hooks on scipy.fft workers) gives the stock kernel's
+    states bit for bit."""
+    import os
+    import sys
+    build_ref = pytest.importorskip("build_ref")
+    if not build_ref.available():
+        pytest.skip("compiled reference kernel not built")
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    from pyqg_gb300.model import grid_constants, spectral_filter
+    from pyqg_gb300.qg_model import qg_inversion_matrix
+    mod = build_ref.load()
+    nx, C2 = 64, bench.C2
+    g = grid_constants(nx, nx, C2["L"], C2["L"])
+    F1 = C2["rd"] ** -2 / (1. + C2["delta"])
+    F2 = C2["delta"] * F1
+    q0 = 1e-7 * np.random.default_rng(4).standard_normal((2, nx, nx))
+    out = []
+    for workers in (0, 4):
+        k = bench._ref_kernel(mod, workers)(2, nx, nx, 1, 0, 0)
+        k.ll, k.kk = g["ll"], g["kk"]
+        k.a = qg_inversion_matrix(g["wv2"], F1, F2)
+        k.Ubg = np.array([C2["U1"], C2["U2"]])
+        k.Qy = np.array([C2["beta"] + F1 * (C2["U1"] - C2["U2"]), C2["beta"] - F2 * (C2["U1"] - C2["U2"])])
+        k.filtr = spectral_filter(g["k"], g["l"], g["dx"], g["dy"], C2["filterfac"])
+        k.rek, k.dt = C2["rek"], 3600.0
+        k.q = q0
+        for _ in range(20):
+            k._invert()
+            k._do_advection()
+            k._do_friction()
+            k._forward_timestep()
+        out.append(np.array(k.q))
+    np.testing.assert_array_equal(out[0], out[1])
