@@ -96,6 +96,13 @@ class Model(PseudoSpectralKernel):
                  diagnostics_list='all', ntd=1, log_level=1, logfile=None):
         ny = nx if ny is None else ny
         W = L if W is None else W
+        if ny != nx:
+            # the reference builds the meridional wavenumbers from nx
+            # (pyqg/model.py:459-460), so its models have wrong wavenumbers
+            # (or index past them) when ny != nx; refuse instead.  The kernel
+            # (PseudoSpectralKernel) itself takes any (ny, nx).
+            raise ValueError("ny != nx is not supported by the model classes (the reference's "
+                             "wavenumber grid assumes ny == nx); got nx=%d, ny=%d" % (nx, ny))
 
         # infer the hook of an explicit parameterization object
         # (pyqg/model.py:203-212)

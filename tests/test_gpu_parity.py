@@ -242,3 +242,49 @@ def test_fixed_engine_unavailable_on_odd_sizes(P, quiet):
     assert m.engine == "fp64"
     with pytest.raises(NotImplementedError):
         m.engine = "fixed"
+
+
+@pytest.mark.parametrize("nx,ny,engines", [(64, 32, ("fp64", "fixed")), (32, 96, ("fp64",))])
+def test_non_square_kernel_vs_oracle(P, nx, ny, engines):
+    """ny != nx at the kernel level (the model classes refuse it, see
+    test_reference_api): wavenumbers of the (ny, nx) grid, stage-by-stage
+    and fused steps of each engine against the oracle after 30 steps, and
+    the fused step bit-identical to the staged one."""
+    import pyqg_oracle as O
+    from pyqg_gb300.kernel import PseudoSpectralKernel
+    from pyqg_gb300.model import spectral_filter
+    from pyqg_gb300.qg_model import qg_inversion_matrix
+    L, W = 1e6, 1e6 * ny / nx
+    kk = 2 * np.pi / L * np.arange(nx // 2 + 1)
+    ll = 2 * np.pi / W * np.append(np.arange(0., ny / 2), np.arange(-ny / 2, 0.))
+    k, l = np.meshgrid(kk, ll)
+    F1 = C1["rd"] ** -2 / (1. + C1["delta"])
+    F2 = C1["delta"] * F1
+    a = qg_inversion_matrix(k ** 2 + l ** 2, F1, F2)
+    filtr = spectral_filter(k, l, L / nx, W / ny, C1["filterfac"])
+    Ubg = np.array([C1["U1"], C1["U2"]])
+    Qy = np.array([C1["beta"] + F1 * (C1["U1"] - C1["U2"]), C1["beta"] - F2 * (C1["U1"] - C1["U2"])])
+    q0 = 1e-7 * np.random.default_rng(12).standard_normal((2, ny, nx))
+
+    def kernel(engine):
+        kn = PseudoSpectralKernel(2, ny, nx)
+        kn.kk, kn.ll, kn.a, kn.Ubg, kn.Qy = kk, ll, a, Ubg, Qy
+        kn.filtr, kn.rek, kn.dt = filtr, C1["rek"], 7200.0
+        kn.engine = engine
+        kn.q = q0
+        return kn
+
+    o = O.OracleKernel(2, ny, nx, a, kk, ll, Ubg, Qy, filtr, C1["rek"], 7200.0)
+    o.set_q(q0)
+    for _ in range(30):
+        o.step()
+    for engine in engines:
+        s, f = kernel(engine), kernel(engine)
+        for _ in range(30):
+            s._invert()
+            s._do_advection()
+            s._do_friction()
+            s._forward_timestep()
+        f._step_fused(30)
+        assert rel_l2(s.q, o.q) < TOL_100, engine
+        np.testing.assert_array_equal(f.q, s.q)

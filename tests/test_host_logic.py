@@ -169,3 +169,12 @@ def test_fused_run_length_stops_at_observation_points():
     # a snapshot predicate ends the batch after the matching step
     m.tavestart, m.log_level = 1e30, 0
     assert Model._fusable_run_length(m, lambda t, tc: tc % 7 == 0) == 3
+
+
+def test_model_refuses_non_square_grid():
+    """The reference's model grid builds ll from nx (pyqg/model.py:459-460):
+    the model classes refuse ny != nx before touching the device."""
+    import pytest
+    import pyqg_gb300 as P
+    with pytest.raises(ValueError, match="ny != nx"):
+        P.QGModel(nx=64, ny=32, log_level=0)
