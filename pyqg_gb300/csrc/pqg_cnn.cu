@@ -264,11 +264,11 @@ struct HaloArgs {
   int* err;
 };
 
-template <int SX, int KS>
+template <int SX, int KS, int KUM>
 __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid_constant__ CUtensorMap tmap, HaloArgs a) {
   constexpr int TXH = 8 * SX + 2 * PAD;
   constexpr int SLAB = TXH * TYH * 16;     // bytes per 8 channels
-  constexpr int CH = KS > 4 ? KS / 4 : 1;  // channel units per tile
+  constexpr int CH = KS > KUM ? KS / KUM : 1;  // channel units per tile (at most 16 KUM channels each)
   constexpr int KU = KS / CH;              // K steps of 16 per unit
   constexpr int cu = 16 * KU, groups = 2 * KU;   // channels and 8-channel slabs per unit
   extern __shared__ __align__(1024) unsigned char csm[];
@@ -1167,6 +1167,7 @@ struct ConvPlan {
   bool halo = false;       // halo kernel (kin % 16 == 0) or gather kernel
   bool rows = false;       // row-tile kernel (width 64; replaces the halo kernel)
   int sx = 0;              // halo kernel tile width / 8
+  int cu = 0;              // halo kernel: input channels per unit (64 or 32)
   int nst = 0;             // halo / row-tile kernel weight stages
   int nh = 0;              // halo / row-tile kernel halo buffers
   int co = 0, nuo = 0;     // row-tile kernel: output channels per unit, units
@@ -1278,7 +1279,12 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
     const size_t budget = 224 * 1024;
     int cap = 4;
     if (const char* e = getenv("PQG_CNN_SX")) cap = std::max(1, atoi(e));
-    const int nu = kin > 64 ? kin / 64 : 1, cu = kin / nu;   // channel units of at most 64
+    // channel units of at most 64 (PQG_CNN_UNIT=32: of at most 32, for a
+    // deeper weight ring beside two halo buffers)
+    int umax = 64;
+    if (const char* e = getenv("PQG_CNN_UNIT")) umax = atoi(e) == 32 ? 32 : 64;
+    const int nu = kin > umax ? kin / umax : 1, cu = kin / nu;
+    c.cu = cu;
     const size_t wb = (size_t)c.N * cu * 2;
     int best = -1;
     for (int sx : {4, 2, 1}) {
@@ -1287,8 +1293,8 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
         const size_t h = (size_t)nh * halo_bytes(sx, cu);
         if (h >= budget) continue;
         int nst, res;
-        if (h + (size_t)NTAP * nu * wb <= budget) { nst = NTAP * nu; res = 1; }
-        else if ((nst = (int)std::min<size_t>(NTAP * nu - 1, (budget - h) / wb)) >= 4) res = 0;
+        if (NTAP * nu <= MAXST && h + (size_t)NTAP * nu * wb <= budget) { nst = NTAP * nu; res = 1; }
+        else if ((nst = (int)std::min<size_t>(std::min(MAXST, NTAP * nu - 1), (budget - h) / wb)) >= 4) res = 0;
         else continue;
         const int score = 4 * sx + 2 * nh + res;
         if (score > best) { best = score; c.sx = sx; c.nh = nh; c.nst = nst; }
@@ -1302,18 +1308,17 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
       if (sscanf(e, "%d,%d", &sx, &nh) == 2 && (sx == 1 || sx == 2 || sx == 4) && (nh == 1 || nh == 2) &&
           W % (8 * sx) == 0 && 2 * sx * c.N <= 512) {
         const size_t h = (size_t)nh * halo_bytes(sx, cu);
-        if (h + (size_t)NTAP * nu * wb <= budget) {
+        if (NTAP * nu <= MAXST && h + (size_t)NTAP * nu * wb <= budget) {
           best = 1; c.sx = sx; c.nh = nh; c.nst = NTAP * nu;
         } else if (h < budget && (budget - h) / wb >= 4) {
-          best = 1; c.sx = sx; c.nh = nh; c.nst = (int)std::min<size_t>(NTAP * nu - 1, (budget - h) / wb);
+          best = 1; c.sx = sx; c.nh = nh;
+          c.nst = (int)std::min<size_t>(std::min(MAXST, NTAP * nu - 1), (budget - h) / wb);
         }
       }
     }
     if (best < 0) c.halo = false;
   }
-  const int nu = kin > 64 ? kin / 64 : 1;
-  c.smem = c.halo ? (size_t)c.nh * halo_bytes(c.sx, kin / nu) + (size_t)c.nst * c.N * (kin / nu) * 2
-                  : gather_smem(c.N);
+  c.smem = c.halo ? (size_t)c.nh * halo_bytes(c.sx, c.cu) + (size_t)c.nst * c.N * c.cu * 2 : gather_smem(c.N);
 }
 
 size_t plan_weight_elems(const ConvPlan& c) {
@@ -1343,14 +1348,16 @@ int encode_map(CUtensorMap* m, const bf16* buf, int C, const pqg_cnn* net, int b
 }
 
 typedef void (*HaloFn)(const __grid_constant__ CUtensorMap, HaloArgs);
-HaloFn halo_kernel(int sx, int ks) {
-#define HK(S)                               \
-  switch (ks) {                             \
-    case 1: return k_conv_halo<S, 1>;       \
-    case 2: return k_conv_halo<S, 2>;       \
-    case 4: return k_conv_halo<S, 4>;       \
-    case 8: return k_conv_halo<S, 8>;       \
-    default: return nullptr;                \
+// ks = input channels / 16, cu = channels per unit (64, or 32 for 64 and
+// 128 input channels)
+HaloFn halo_kernel(int sx, int ks, int cu) {
+#define HK(S)                                                              \
+  switch (ks) {                                                            \
+    case 1: return k_conv_halo<S, 1, 4>;                                   \
+    case 2: return k_conv_halo<S, 2, 4>;                                   \
+    case 4: return cu == 32 ? k_conv_halo<S, 4, 2> : k_conv_halo<S, 4, 4>; \
+    case 8: return cu == 32 ? k_conv_halo<S, 8, 2> : k_conv_halo<S, 8, 4>; \
+    default: return nullptr;                                               \
   }
   if (sx == 4) { HK(4) }
   if (sx == 2) { HK(2) }
@@ -1417,7 +1424,7 @@ int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int
     a.e = e;
     a.err = net->err;
     const dim3 grid(std::min(a.ntiles, net->nsm * net->cps));
-    auto fn = halo_kernel(c.sx, c.kin / 16);
+    auto fn = halo_kernel(c.sx, c.kin / 16, c.cu);
     if (!fn) return cfail(PQG_ERR_UNSUPPORTED, "no convolution kernel for this channel count");
     fn<<<grid, 32 * (NEPI + 1 + c.sx), c.smem, st>>>(m, a);
   } else {
@@ -1477,7 +1484,9 @@ int set_attrs() {
   const int big = optin - 2048;
   for (int sx : {1, 2, 4})
     for (int ks : {1, 2, 4, 8})
-      CCUDA(cudaFuncSetAttribute(halo_kernel(sx, ks), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      for (int cu : {64, 32})
+        if (cu == 64 || ks >= 4)
+          CCUDA(cudaFuncSetAttribute(halo_kernel(sx, ks, cu), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   for (int kin : {16, 32, 64, 128})
     for (bool small : {false, true})
       CCUDA(cudaFuncSetAttribute(rows_kernel(kin, small), cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 12288));
@@ -1500,7 +1509,7 @@ int repack(pqg_cnn* net, cudaStream_t st) {
                                                                     c.nun, c.kin, c.ch, c.nuo);
       else if (c.halo)
         k_pack_taps<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w, c.N,
-                                                                   c.kin, c.kin > 64 ? c.kin / 64 : 1);
+                                                                   c.kin, c.kin / c.cu);
       else
         k_pack_chunks<<<grid_for(plan_weight_elems(c)), 256, 0, st>>>(net->params + l.woff, l.cin, l.cout, d, c.w,
                                                                      c.N, c.nchunk);
