@@ -51,13 +51,15 @@ def _truncate_physical(q, nc):
     return np.fft.irfftn(out * (nc * nc) / (nf * nf), s=(nc, nc), axes=(-2, -1))
 
 
-def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None):
+def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None, schedule="constant"):
     """Adam on standardised tensors X, Y (N, C, ny, nx); returns the mean
     loss of every epoch.  A network without normalisation layers can
     collapse at lr 1e-3 (all ReLUs dead: the loss jumps back to the variance
     of the target); the best parameters are kept, and after an epoch whose
     loss exceeds 1.5 times the best (or reaches 0.99) they are restored and
-    the learning rate is halved."""
+    the learning rate is halved.  schedule "cosine" decays the rate of every
+    epoch as lr (1 + cos(pi e / epochs)) / 2 (times the halvings)."""
+    import math
     import torch
     g = torch.Generator(device="cpu").manual_seed(seed)
     n = X.shape[0] - X.shape[0] % batch
@@ -66,12 +68,13 @@ def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None):
     for ep in range(epochs):
         perm = torch.randperm(X.shape[0], generator=g)[:n].to(X.device)
         tot = 0.0
+        lr_ep = lr * (0.5 * (1.0 + math.cos(math.pi * ep / epochs)) if schedule == "cosine" else 1.0)
         for i in range(0, n, batch):
             idx = perm[i:i + batch]
-            tot += net.train_step(X[idx].contiguous(), Y[idx].contiguous(), lr=lr)
+            tot += net.train_step(X[idx].contiguous(), Y[idx].contiguous(), lr=lr_ep)
         hist.append(tot / (n // batch))
         if log:
-            log("epoch %d loss %.4f lr %.2e" % (ep, hist[-1], lr))
+            log("epoch %d loss %.4f lr %.2e" % (ep, hist[-1], lr_ep))
         if hist[-1] < best:
             best, best_p = hist[-1], net.params
         elif best_p is not None and (hist[-1] > 1.5 * best or hist[-1] >= 0.99):
@@ -85,7 +88,7 @@ def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None):
 
 
 def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30, batch=64, lr=1e-3,
-        eval_years=3.0, spectra_every=240, seed0=2000, scales=(1.0, 0.5), log=print):
+        eval_years=3.0, spectra_every=240, seed0=2000, scales=(1.0, 0.5), lr_schedule="constant", log=print):
     import torch
     import pyqg_gb300 as P
     from .closure import CNNParameterization, ConvNet
@@ -94,7 +97,7 @@ def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30
     report = {"config": dict(nruns=nruns, spinup_years=spinup_years, sample_years=sample_years,
                              sample_every_steps=sample_every, epochs=epochs, batch=batch, lr=lr,
                              eval_years=eval_years, seed0=seed0, dt_fine=dt_f, dt_coarse=dt_c,
-                             closure_scales=list(scales))}
+                             closure_scales=list(scales), lr_schedule=lr_schedule)}
     spin = int(round(spinup_years * YEAR / dt_f))
     nsnap = max(1, int(round(sample_years * YEAR / dt_f / sample_every)))
     X, Y, ens_f = generate_training_data(nruns=nruns, nx_fine=256, nx_coarse=64, dt=dt_f, spinup_steps=spin,
@@ -112,7 +115,7 @@ def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30
     n_val = max(batch, X.shape[0] // 10)
     net = ConvNet(max_batch=max(batch, nruns), seed=seed0)
     t1 = time.time()
-    hist = train(net, Xs[n_val:], Ys[n_val:], epochs, batch=batch, lr=lr, log=log)
+    hist = train(net, Xs[n_val:], Ys[n_val:], epochs, batch=batch, lr=lr, log=log, schedule=lr_schedule)
     torch.cuda.synchronize()
     # validation: relative MSE of the standardised forcing on held-out samples
     pred = torch.empty_like(Ys[:n_val])
@@ -228,11 +231,12 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--eval-years", type=float, default=3.0)
     ap.add_argument("--scales", default="1.0,0.5", help="closure amplitudes to evaluate online")
+    ap.add_argument("--lr-schedule", default="constant", choices=["constant", "cosine"])
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     rep = run(nruns=a.nruns, spinup_years=a.spinup_years, sample_years=a.sample_years,
               sample_every=a.sample_every, epochs=a.epochs, eval_years=a.eval_years,
-              scales=tuple(float(x) for x in a.scales.split(",")))
+              scales=tuple(float(x) for x in a.scales.split(",")), lr_schedule=a.lr_schedule)
     txt = json.dumps(rep)
     print(txt)
     if a.out:
