@@ -1,7 +1,7 @@
 """CPU oracle of the spectral coarse-graining and subgrid forcing.
 
-TEST INFRASTRUCTURE ONLY: imported by ``tests/`` as the checker, never by
-the product path.
+TEST INFRASTRUCTURE ONLY: imported by ``tests/`` to compare against, never
+by the product path.
 
 Parity unpinned: the reference has no coarse-graining (its
 ``Model.subgrid_forcing`` raises, ``pyqg/model.py:397-402``).  This numpy

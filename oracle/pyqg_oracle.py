@@ -1,8 +1,8 @@
 """CPU oracle: a numpy restatement of pyqg's pseudo-spectral time step.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and
-``bench.py``'s CPU-baseline leg may import this module, and only as the checker
-(or as the timed CPU baseline); the product path never calls it.
+``bench.py``'s CPU-baseline leg may import this module, and only to compare
+against (or as the timed CPU baseline); the product path never calls it.
 
 Each function restates one stage of the reference ``PseudoSpectralKernel``
 (``pyqg/kernel.pyx``) with the same arithmetic order, using ``numpy.fft``
