@@ -88,7 +88,7 @@ def train(net, X, Y, epochs, batch=64, lr=1e-3, seed=0, log=None, schedule="cons
 
 
 def run(nruns=32, spinup_years=4.0, sample_years=1.0, sample_every=48, epochs=30, batch=64, lr=1e-3,
-        eval_years=3.0, spectra_every=240, seed0=2000, scales=(1.0, 0.5), lr_schedule="constant", log=print):
+        eval_years=3.0, spectra_every=240, seed0=2000, scales=(1.0, 0.5), lr_schedule="cosine", log=print):
     import torch
     import pyqg_gb300 as P
     from .closure import CNNParameterization, ConvNet
@@ -231,7 +231,7 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--eval-years", type=float, default=3.0)
     ap.add_argument("--scales", default="1.0,0.5", help="closure amplitudes to evaluate online")
-    ap.add_argument("--lr-schedule", default="constant", choices=["constant", "cosine"])
+    ap.add_argument("--lr-schedule", default="cosine", choices=["constant", "cosine"])
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     rep = run(nruns=a.nruns, spinup_years=a.spinup_years, sample_years=a.sample_years,
