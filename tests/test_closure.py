@@ -277,12 +277,14 @@ def test_default_net_learns():
 def test_row_tile_and_halo_kernels_agree(channels, batch, monkeypatch):
     """The row-tile kernel (horizontal taps folded into N) on every layer it
     takes, the default choice, and the halo kernel (one MMA per tap) on
-    every layer, on the same network: forward and gradients."""
+    every layer with 64- and with 32-channel input units, on the same
+    network: forward and gradients."""
     import torch
     from pyqg_gb300.closure import ConvNet
     nets = []
-    for rows in ("2", "1", "0"):
+    for rows, unit in (("2", "64"), ("1", "64"), ("0", "64"), ("0", "32")):
         monkeypatch.setenv("PQG_CNN_ROWS", rows)
+        monkeypatch.setenv("PQG_CNN_UNIT", unit)   # halo kernel: input channels per unit
         nets.append(ConvNet(channels, max_batch=batch, seed=13))
     p = _he_params(nets[0], 13)
     rng = np.random.default_rng(13)
