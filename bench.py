@@ -576,12 +576,19 @@ def ensemble_throughput(args):
     nbytes = 40 * S + 8 * Pn
     hbm, kind = peaks()
     ach = nbytes / (ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("ensemble_config3_step")
+    except Exception:
+        traffic = None
     return {"workload": "config 3: 1024 FP32 members (614 x nx=64, 307 x nx=128, 103 x nx=256, "
                         "20 % three-layer), uneven beta / rek, autotuned, CUDA graphs",
             "ms_per_ensemble_step": ms, "member_steps_per_s": len(members) / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                         "algorithmic_bytes_per_step": nbytes, "peak_source": kind,
-                         "note": "compulsory bytes 40 S + 8 P (FP32) per ensemble step"}}
+                         "algorithmic_bytes_per_step": nbytes, "peak_source": kind, "traffic": traffic,
+                         "note": "compulsory bytes 40 S + 8 P (FP32) per ensemble step; traffic = measured "
+                                 "DRAM bytes of one steady step (ncu, serialised launches)"}}
 
 
 def profile_case(args):
