@@ -1168,6 +1168,7 @@ struct ConvPlan {
   bool rows = false;       // row-tile kernel (width 64; replaces the halo kernel)
   int sx = 0;              // halo kernel tile width / 8
   int cu = 0;              // halo kernel: input channels per unit (64 or 32)
+  int cps = 0;             // halo kernel: persistent CTAs per SM (0: the network's)
   int nst = 0;             // halo / row-tile kernel weight stages
   int nh = 0;              // halo / row-tile kernel halo buffers
   int co = 0, nuo = 0;     // row-tile kernel: output channels per unit, units
@@ -1300,12 +1301,15 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
         if (score > best) { best = score; c.sx = sx; c.nh = nh; c.nst = nst; }
       }
     }
-    // tuning override for one layer shape: PQG_CNN_HALO_<kin>_<nout>=<sx>,<nh>
+    // tuning override for one layer shape:
+    // PQG_CNN_HALO_<kin>_<nout>=<sx>,<nh>[,<CTAs per SM>]
     char key[64];
     snprintf(key, sizeof key, "PQG_CNN_HALO_%d_%d", kin, nout);
     if (const char* e = getenv(key)) {
-      int sx = 0, nh = 0;
-      if (sscanf(e, "%d,%d", &sx, &nh) == 2 && (sx == 1 || sx == 2 || sx == 4) && (nh == 1 || nh == 2) &&
+      int sx = 0, nh = 0, cps = 0;
+      const int nread = sscanf(e, "%d,%d,%d", &sx, &nh, &cps);
+      if (nread == 3 && cps >= 1 && cps <= 4) c.cps = cps;
+      if (nread >= 2 && (sx == 1 || sx == 2 || sx == 4) && (nh == 1 || nh == 2) &&
           W % (8 * sx) == 0 && 2 * sx * c.N <= 512) {
         const size_t h = (size_t)nh * halo_bytes(sx, cu);
         if (NTAP * nu <= MAXST && h + (size_t)NTAP * nu * wb <= budget) {
@@ -1423,7 +1427,7 @@ int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int
     a.g = net->g;
     a.e = e;
     a.err = net->err;
-    const dim3 grid(std::min(a.ntiles, net->nsm * net->cps));
+    const dim3 grid(std::min(a.ntiles, net->nsm * (c.cps ? c.cps : net->cps)));
     auto fn = halo_kernel(c.sx, c.kin / 16, c.cu);
     if (!fn) return cfail(PQG_ERR_UNSUPPORTED, "no convolution kernel for this channel count");
     fn<<<grid, 32 * (NEPI + 1 + c.sx), c.smem, st>>>(m, a);
