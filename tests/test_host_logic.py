@@ -178,3 +178,32 @@ def test_model_refuses_non_square_grid():
     import pyqg_gb300 as P
     with pytest.raises(ValueError, match="ny != nx"):
         P.QGModel(nx=64, ny=32, log_level=0)
+
+
+def test_header_compiles_as_c_and_links(tmp_path):
+    """include/pyqg_gb300.h is plain C99 (the reference-side FFI binds it
+    from C): a C program compiles against it, links the library and calls
+    entry points that need no GPU."""
+    import os
+    import shutil
+    import subprocess
+    import pytest
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.join(root, "pyqg_gb300", "lib")
+    if not os.path.exists(os.path.join(libdir, "libpyqg_gb300.so")):
+        pytest.skip("library not built")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "pyqg_gb300.h"\n#include <stdio.h>\n'
+                   'int main(void) {\n'
+                   '  int v = pqg_version();\n'
+                   '  const char *e = pqg_last_error();\n'
+                   '  printf("%d %d\\n", v > 0, e != 0);\n'
+                   '  return 0;\n}\n')
+    exe = tmp_path / "use_header"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    os.path.join(root, "include"), str(src), "-L", libdir, "-lpyqg_gb300",
+                    "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out == ["1", "1"]
