@@ -273,6 +273,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
   constexpr int cu = 16 * KU, groups = 2 * KU;   // channels and 8-channel slabs per unit
   extern __shared__ __align__(1024) unsigned char csm[];
   __shared__ __align__(8) uint64_t hfull[2], hempty[2], afull[2], aempty[2], wfull[MAXST], wempty[MAXST];
+  __shared__ __align__(8) uint64_t drain[SX];   // failure path: the MMAs of each issuer
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
   __shared__ __align__(16) float s_bias[256];
@@ -298,6 +299,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
       tc::mbar_init(&wfull[s], 1);
       tc::mbar_init(&wempty[s], SX);
     }
+    for (int i = 0; i < SX; i++) tc::mbar_init(&drain[i], 1);
     tc::mbar_fence_init();
     s_fail = 0;
   }
@@ -433,9 +435,14 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
   if (!ok) s_fail = 1;
   __syncthreads();
   if (s_fail) {
+    // every issuer waits (bounded) for its own MMAs, and the copies still in
+    // flight get a bounded time, before TMEM is freed
+    if (warp > NEPI && lane == 0) {
+      tc::mma_commit(&drain[warp - NEPI - 1]);
+      tc::mbar_wait(&drain[warp - NEPI - 1], 0, 10000000ull);
+    }
     if (tid == 0) {
       atomicExch(a.err, 1);
-      // give copies and MMAs still in flight a bounded time before TMEM is freed
       tc::mbar_wait(&hfull[0], 0, 10000000ull);
       tc::mbar_wait(&hfull[1], 0, 10000000ull);
     }
@@ -536,6 +543,7 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
   __shared__ __align__(8) uint64_t hfull[RMAXH], hempty[RMAXH], afull[RNACC], aempty[RNACC], wfull[RMAXST],
       wempty[RMAXST];
   __shared__ __align__(8) uint64_t xbar[2][REPI / 2];
+  __shared__ __align__(8) uint64_t drain;   // failure path: the issuer's MMAs
   __shared__ __align__(16) float xbuf[2][REPI][4][16];   // edge values swapped between the two warps of a row
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
@@ -557,6 +565,7 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
     }
     for (int i = 0; i < 2; i++)
       for (int p = 0; p < REPI / 2; p++) tc::mbar_init(&xbar[i][p], 64);
+    tc::mbar_init(&drain, 1);
     for (int i = 0; i < NACC; i++) {
       tc::mbar_init(&afull[i], 1);
       tc::mbar_init(&aempty[i], 32 * REPI);
@@ -771,11 +780,15 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
   if (!ok) s_fail = 1;
   __syncthreads();
   if (s_fail) {
+    // the issuer waits (bounded) for its own MMAs, and the copies still in
+    // flight get a bounded time, before TMEM is freed
+    if (warp == REPI + 1 && lane == 0) {
+      tc::mma_commit(&drain);
+      tc::mbar_wait(&drain, 0, 10000000ull);
+    }
     if (tid == 0) {
       atomicExch(a.err, 1);
-      // give copies and MMAs still in flight a bounded time before TMEM is freed
-      tc::mbar_wait(&hfull[0], 0, 10000000ull);
-      tc::mbar_wait(&hfull[1], 0, 10000000ull);
+      for (int i = 0; i < NH; i++) tc::mbar_wait(&hfull[i], 0, 10000000ull);
     }
     __syncthreads();
   }
