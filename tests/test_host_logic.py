@@ -207,3 +207,23 @@ def test_header_compiles_as_c_and_links(tmp_path):
                     "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert out == ["1", "1"]
+
+
+def test_reference_arm_prints_its_json_line():
+    """`bench.py --impl reference` runs on the host alone: one JSON line with
+    the metric, impl, cpu_baseline (kind, cores, sample), e2e and no GPU
+    launches."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "1", "--chunk", "5"],
+                         cwd=root, check=True, capture_output=True, text=True, timeout=600).stdout
+    line = json.loads(out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "sim-yr/hr" and line["value"] > 0
+    assert line["gpu_launches"] == 0
+    assert set(line["cpu_baseline"]) >= {"value", "unit", "cores", "kind", "sample"}
+    assert line["cpu_baseline"]["kind"] in ("reference", "port")
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
