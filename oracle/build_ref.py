@@ -10,16 +10,26 @@ with the reference's numpy.fft fallback selected (``PYQG_USE_PYFFTW = 0``,
 ``pyqg/kernel.pyx:13-19,245-267``; pyFFTW/FFTW are not available here).  All
 outputs go to ``oracle/_ref/`` which is git-ignored.
 
-Two stages, so that the result can also be built on a machine without the
+The reference tree is located by the environment variable
+``PYQG_REFERENCE_ROOT`` (the directory holding ``pyqg/kernel.pyx``); without
+it the stages that need the tree are skipped.
+
+Three stages, so that the result can also be built on a machine without the
 reference tree or Cython:
 
 ``cythonize``  needs the reference tree and Cython.  Writes
                ``oracle/_ref/pyqg_ref_kernel.c`` (generated C).
+``stage``      needs the reference tree.  Copies the reference package's
+               Python modules (``pyqg/*.py``, not its tests or kernel) to
+               ``oracle/_ref/pyqg_src/pyqg/``, so that tests can run the
+               unchanged ``pyqg.Model`` classes over another kernel module on
+               a machine without the tree.
 ``compile``    needs gcc, the Python headers and numpy.  Compiles that C file
                with ``-O3 -fopenmp`` (``setup.py:77-124`` of the reference uses
                ``-fopenmp`` the same way) into ``oracle/_ref/pyqg_ref_kernel*.so``.
 
-Usage: ``python oracle/build_ref.py [cythonize] [compile]`` (both by default).
+Usage: ``python oracle/build_ref.py [cythonize] [stage] [compile]`` (all by
+default).
 """
 import os
 import shutil
@@ -29,10 +39,23 @@ import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("PYQG_REFERENCE_ROOT", "/root/reference")
-REF_KERNEL = os.path.join(REF_ROOT, "pyqg", "kernel.pyx")
+REF_ROOT = os.environ.get("PYQG_REFERENCE_ROOT", "")
+REF_KERNEL = os.path.join(REF_ROOT, "pyqg", "kernel.pyx") if REF_ROOT else ""
 MODNAME = "pyqg_ref_kernel"
 C_FILE = os.path.join(OUT, MODNAME + ".c")
+STAGED = os.path.join(OUT, "pyqg_src")   # staged reference Python package
+
+
+def tree_available():
+    return bool(REF_KERNEL) and os.path.exists(REF_KERNEL)
+
+
+def require_tree():
+    if not REF_ROOT:
+        raise FileNotFoundError("PYQG_REFERENCE_ROOT is not set: it must name the "
+                                "directory that holds the reference's pyqg/kernel.pyx")
+    if not os.path.exists(REF_KERNEL):
+        raise FileNotFoundError("PYQG_REFERENCE_ROOT=%s holds no pyqg/kernel.pyx" % REF_ROOT)
 
 
 def so_path():
@@ -42,8 +65,7 @@ def so_path():
 
 def cythonize():
     """Generate C from the reference kernel.pyx (numpy.fft fallback)."""
-    if not os.path.exists(REF_KERNEL):
-        raise FileNotFoundError(REF_KERNEL)
+    require_tree()
     os.makedirs(OUT, exist_ok=True)
     inc = os.path.join(OUT, "include")
     os.makedirs(inc, exist_ok=True)
@@ -55,6 +77,24 @@ def cythonize():
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
                    stderr=subprocess.PIPE)
     return C_FILE
+
+
+def stage_python():
+    """Copy the reference package's Python modules into oracle/_ref."""
+    require_tree()
+    src = os.path.join(REF_ROOT, "pyqg")
+    dst = os.path.join(STAGED, "pyqg")
+    if os.path.exists(dst):
+        shutil.rmtree(dst)
+    os.makedirs(dst)
+    for name in sorted(os.listdir(src)):
+        if name.endswith(".py"):
+            shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
+    return dst
+
+
+def staged_available():
+    return os.path.exists(os.path.join(STAGED, "pyqg", "model.py"))
 
 
 def compile_c():
@@ -99,8 +139,9 @@ def build(quiet=True):
     Returns the path of the built module or None when it cannot be built.
     """
     try:
-        if os.path.exists(REF_KERNEL):
+        if tree_available():
             cythonize()
+            stage_python()
         if os.path.exists(C_FILE):
             return compile_c()
     except (subprocess.CalledProcessError, RuntimeError, OSError) as e:
@@ -113,8 +154,10 @@ def build(quiet=True):
 
 
 if __name__ == "__main__":
-    stages = sys.argv[1:] or ["cythonize", "compile"]
+    stages = sys.argv[1:] or ["cythonize", "stage", "compile"]
     if "cythonize" in stages:
         print(cythonize())
+    if "stage" in stages:
+        print(stage_python())
     if "compile" in stages:
         print(compile_c())

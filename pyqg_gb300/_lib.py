@@ -17,6 +17,7 @@ PQG_ERR_CUDA = 3
 PQG_ERR_NOMEM = 4
 PQG_ERR_STATE = 5
 PQG_ERR_TIMEOUT = 6
+PQG_NOALLOC_MAX_COMPLEX = 1 << 19   # scratch limit of pqg_rfft2_noalloc
 
 _P = ctypes.c_void_p
 _D = ctypes.c_double

@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
   __shared__ __align__(8) uint64_t drain[SX];   // failure path: the MMAs of each issuer
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
+  __shared__ long long s_issued[2];   // copies the producer issued: halo units, weight blocks
   __shared__ __align__(16) float s_bias[256];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int N = a.N, NST = a.nst, NH = a.nh;
@@ -302,6 +303,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
     for (int i = 0; i < SX; i++) tc::mbar_init(&drain[i], 1);
     tc::mbar_fence_init();
     s_fail = 0;
+    s_issued[0] = s_issued[1] = 0;
   }
   for (int i = tid; i < N; i += blockDim.x) s_bias[i] = (a.e.bias && i < a.e.cout) ? a.e.bias[i] : 0.f;
   tc::fence_before();
@@ -342,6 +344,8 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
           }
         }
       }
+      s_issued[0] = u;
+      s_issued[1] = resident ? (u > 0 ? NTAP * CH : 0) : wq;
     }
     __syncwarp();
   } else if (warp > NEPI) {
@@ -443,8 +447,8 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
     }
     if (tid == 0) {
       atomicExch(a.err, 1);
-      tc::mbar_wait(&hfull[0], 0, 10000000ull);
-      tc::mbar_wait(&hfull[1], 0, 10000000ull);
+      tc::drain_ring(hfull, NH, s_issued[0], 10000000ull);
+      tc::drain_ring(wfull, resident ? NTAP * CH : NST, s_issued[1], 10000000ull);
     }
     __syncthreads();
   }
@@ -547,6 +551,7 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
   __shared__ __align__(16) float xbuf[2][REPI][4][16];   // edge values swapped between the two warps of a row
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
+  __shared__ long long s_issued[2];   // copies the producer issued: halo units, weight blocks
   __shared__ __align__(16) float s_bias[128];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int Nu = a.Nu, CO = a.CO, NUO = a.nuo, NST = a.nst, NH = a.nh, NACC = a.nacc;
@@ -576,6 +581,7 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
     }
     tc::mbar_fence_init();
     s_fail = 0;
+    s_issued[0] = s_issued[1] = 0;
   }
   for (int i = tid; i < 128; i += blockDim.x) s_bias[i] = (a.e.bias && i < a.e.cout) ? a.e.bias[i] : 0.f;
   tc::fence_before();
@@ -624,6 +630,8 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
           }
         }
       }
+      s_issued[0] = hq;
+      s_issued[1] = resident ? (first ? 0 : nblk) : wq;
     }
     __syncwarp();
   } else if (warp == REPI + 1) {
@@ -788,7 +796,8 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
     }
     if (tid == 0) {
       atomicExch(a.err, 1);
-      for (int i = 0; i < NH; i++) tc::mbar_wait(&hfull[i], 0, 10000000ull);
+      tc::drain_ring(hfull, NH, s_issued[0], 10000000ull);
+      tc::drain_ring(wfull, resident ? nblk : NST, s_issued[1], 10000000ull);
     }
     __syncthreads();
   }
@@ -836,12 +845,14 @@ __global__ void __launch_bounds__(128) k_conv_gather(GatherArgs a) {
   const int HW = a.g.H * a.g.W;
   const int b = p / HW, rem = p - b * HW, y = rem / a.g.W, x = rem - (rem / a.g.W) * a.g.W;
   bool failed = false;
+  int issued = 0;   // MMA commits issued (one per chunk)
   for (int c = 0; c < a.nchunk; c++) {
     const int s = c & 1;
     if (c >= 2) {
       const bool to = !tc::mbar_wait(&mbar[s], ((c - 2) >> 1) & 1);
       if (__syncthreads_or(to)) { failed = true; break; }
     }
+    issued = c + 1;
     unsigned char* sA = sA0 + s * CHUNK_A;
     unsigned char* sB = sB0 + s * bbytes;
 #pragma unroll 1
@@ -881,8 +892,7 @@ __global__ void __launch_bounds__(128) k_conv_gather(GatherArgs a) {
   }
   if (failed) {
     if (tid == 0) atomicExch(a.err, 1);
-    tc::mbar_wait(&mbar[0], 0, 10000000ull);
-    tc::mbar_wait(&mbar[1], 0, 10000000ull);
+    tc::drain_ring(mbar, 2, issued, 10000000ull);
   } else {
     tc::fence_after();
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
@@ -940,12 +950,14 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
   const int r1 = min(a.nrows, r0 + a.rows_per_cta);
   const int nchunk = r1 - r0;
   bool failed = false;
+  int issued = 0;   // MMA commits issued (one per chunk)
   for (int c = 0; c < nchunk; c++) {
     const int s = c & 1;
     if (c >= 2) {
       const bool to = !tc::mbar_wait(&mbar[s], ((c - 2) >> 1) & 1);
       if (__syncthreads_or(to)) { failed = true; break; }
     }
+    issued = c + 1;
     unsigned char* sA = sA0 + s * CHUNK_A;
     unsigned char* sB = sB0 + s * bbytes;
     const int rr = r0 + c;
@@ -1014,8 +1026,7 @@ __global__ void __launch_bounds__(128) k_wgrad(WgradArgs a) {
   }
   if (failed) {
     if (tid == 0) atomicExch(a.err, 1);
-    tc::mbar_wait(&mbar[0], 0, 10000000ull);
-    tc::mbar_wait(&mbar[1], 0, 10000000ull);
+    tc::drain_ring(mbar, 2, issued, 10000000ull);
   } else if (nchunk > 0) {
     tc::fence_after();
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);

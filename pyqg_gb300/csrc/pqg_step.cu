@@ -1301,9 +1301,26 @@ static void ab_coeffs(int ablevel, double dt, double& c1, double& c2, double& c3
   else { c1 = 23. / 12. * dt; c2 = -16. / 12. * dt; c3 = 5. / 12. * dt; }
 }
 
+// cudaFuncSetAttribute acts on the current device only, so the limits are
+// raised once per device ordinal (under a lock: plans may be created from
+// several host threads).
+static std::mutex g_smem_mutex;
+static bool g_smem_done[64];
+
+static int set_smem_limits_current();
+
 static int set_smem_limits() {
-  static bool done = false;
-  if (done) return PQG_OK;
+  int dev = 0;
+  PQG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(PQG_ERR_UNSUPPORTED, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_smem_mutex);
+  if (g_smem_done[dev]) return PQG_OK;
+  const int rc = set_smem_limits_current();
+  if (rc == PQG_OK) g_smem_done[dev] = true;
+  return rc;
+}
+
+static int set_smem_limits_current() {
   const int big = 200 * 1024;
   for (int m = 8; m <= 1024; m *= 2)
     PQG_CUDA(cudaFuncSetAttribute(row_adv_kernel(m), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -1334,7 +1351,6 @@ static int set_smem_limits() {
   }
   PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(3), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PQG_CUDA(cudaFuncSetAttribute(col_fused_kernel(3), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  done = true;
   return PQG_OK;
 }
 
@@ -1871,8 +1887,11 @@ PQG_API int pqg_rfft2_noalloc(const double* x, double* xh, int nplanes, int ny, 
   PQG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(PQG_ERR_UNSUPPORTED, "device ordinal out of range");
   cudaStream_t st = (cudaStream_t)stream;
+  // The lock is held until both kernels are queued: a call from another
+  // host thread on the same stream that uploads other twiddle tables is
+  // then ordered behind this call's kernels.
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     NoAllocDevice& d = g_noalloc_dev[dev];
     if (!d.ready) {
       // once per device, with that device current: host-side names of the

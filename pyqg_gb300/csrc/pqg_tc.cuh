@@ -112,6 +112,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint6
   }
 }
 
+// Failure path of a pipeline: wait (bounded) for the last asynchronous copy
+// issued on each barrier of a ring of `n` barriers that received `issued`
+// copies in round-robin order.  Copy j lands on barrier j % n and completes
+// that barrier's phase j / n; copies on one barrier complete in order, so
+// the last one suffices.
+__device__ __forceinline__ void drain_ring(uint64_t* bars, int n, long long issued, uint64_t limit_ns) {
+  for (int i = 0; i < n && i < issued; i++) {
+    const long long last = i + ((issued - 1 - i) / n) * n;
+    mbar_wait(&bars[i], (uint32_t)((last / n) & 1), limit_ns);
+  }
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(mbar)) : "memory");
 }

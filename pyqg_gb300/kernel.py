@@ -647,3 +647,35 @@ for _n in ("ph", "u", "v", "uh", "vh", "uq", "vq", "uqh", "vqh", "dqh", "duh",
     setattr(PseudoSpectralKernel, _n, _field_property(_n))
 
 _PRE_INIT = ("Ubg", "Qy", "a", "kk", "ll", "filtr", "rek", "dt", "q", "qh")
+
+
+# ---------------------------------------------------------------------------
+# Module-level time-stepping helpers (pyqg/kernel.pyx:640-663).  pyqg's
+# Model imports them from its kernel module (pyqg/model.py:8), so they are
+# part of the module's interface; they act on host complex arrays, typed as
+# the reference's (double dt, complex128 arrays of three dimensions).
+# ---------------------------------------------------------------------------
+def _tendency_args(dt, *arrays):
+    dt = float(dt)
+    for i, x in enumerate(arrays):
+        _check_array(x, np.complex128, 3, "dqdt" + "_p" * i)
+    return dt
+
+
+def tendency_forward_euler(dt, dqdt):
+    """Forward Euler tendency dt * dqdt."""
+    dt = _tendency_args(dt, dqdt)
+    return dt * dqdt
+
+
+def tendency_ab2(dt, dqdt, dqdt_p):
+    """Second-order Adams-Bashforth tendency."""
+    dt = _tendency_args(dt, dqdt, dqdt_p)
+    return (1.5 * dt) * dqdt + (-0.5 * dt) * dqdt_p
+
+
+def tendency_ab3(dt, dqdt, dqdt_p, dqdt_pp):
+    """Third-order Adams-Bashforth tendency."""
+    dt = _tendency_args(dt, dqdt, dqdt_p, dqdt_pp)
+    return ((23 / 12. * dt) * dqdt + (-16 / 12. * dt) * dqdt_p
+            + (5 / 12. * dt) * dqdt_pp)

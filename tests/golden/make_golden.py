@@ -3,7 +3,7 @@
 Run in a container that has the reference tree (it imports the reference
 package in place and its Cython kernel compiled by ``oracle/build_ref.py``):
 
-    python tests/golden/make_golden.py
+    PYQG_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py [prefix ...]
 
 Every fixture holds the reference's own constants, inputs and outputs for a
 seeded case, so the CPU oracle and the GPU path can be checked against the
@@ -63,7 +63,9 @@ def run_case(m, q0, steps, stage_step1=True, q_param=None):
     return out
 
 
-def main():
+def main(only=None):
+    """Write every fixture, or those whose file names start with one of
+    ``only`` (e.g. ``params diag``)."""
     pyqg = import_reference_pyqg()
     rng = np.random.default_rng
     files = {}
@@ -144,12 +146,101 @@ def main():
          for k, v in params.items()}))
     files["layered_fixture_nx64.npz"] = rec
 
+    files.update(physical_parameterizations(pyqg))
+    files.update(diagnostics(pyqg))
+    save(files, only)
+
+
+def save(files, only=None):
     for name, rec in files.items():
+        if only and not any(name.startswith(o) for o in only):
+            continue
         np.savez_compressed(os.path.join(HERE, name), **rec)
         print(name, os.path.getsize(os.path.join(HERE, name)))
+
+
+def physical_parameterizations(pyqg):
+    """The reference's Smagorinsky, BackscatterBiharmonic, ZannaBolton2020
+    and RingForcing (pyqg/parameterizations.py:132-366) evaluated on a
+    seeded state of config-1 physics at nx=32 after 10 steps, with u, v and ph refreshed from
+    that state by one inversion."""
+    c1 = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+              U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
+    m = pyqg.QGModel(**dict(c1, nx=32), **QUIET)
+    m.q = 1e-6 * np.random.default_rng(3).standard_normal((2, 32, 32))
+    for _ in range(10):
+        m._step_forward()
+    m._invert()
+    rec = dict(q=np.asarray(m.q).copy(), ph=np.asarray(m.ph).copy(),
+               u=np.asarray(m.u).copy(), v=np.asarray(m.v).copy(),
+               dx=np.float64(m.dx), Hi=np.asarray(m.Hi).copy())
+    rec.update(consts(m))
+    rec["smag_du"], rec["smag_dv"] = pyqg.Smagorinsky()(m)
+    rec["smag_nu"] = pyqg.Smagorinsky()(m, just_viscosity=True)
+    rec["smag02_du"], rec["smag02_dv"] = pyqg.Smagorinsky(constant=0.2)(m)
+    rec["back_dq"] = pyqg.BackscatterBiharmonic()(m)
+    rec["back05_dq"] = pyqg.BackscatterBiharmonic(smag_constant=0.1, back_constant=0.5)(m)
+    rec["zb_du"], rec["zb_dv"] = pyqg.ZannaBolton2020()(m)
+    ring = dict(k_in_forc=2e-5, k_out_forc=6e-5, mag_noise_forc=3.0)
+    for i, layers in enumerate(("all", "surf", "bottom")):
+        np.random.seed(100 + i)
+        rec["ring_%s_dq" % layers] = pyqg.RingForcing(layers=layers, **ring)(m)
+    rec["ring_seeds"] = np.array([100, 101, 102])
+    return {"params_physical_nx32.npz": rec}
+
+
+def _numpy1_modal_projection(self, p, forward=True):
+    """pyqg/model.py:307-317 with numpy 1's reading of its ``solve`` call.
+
+    The reference solves ``pmodes x = p[:, l, k]`` for every wavenumber by
+    passing ``p.T`` of shape (nk, nl, nz) as a stack of vectors; numpy 2
+    reads a right-hand side of more than one dimension as matrices, and the
+    call fails.  The same solves are written here with an explicit vector
+    axis; nothing else of the reference is changed."""
+    if forward:
+        return np.linalg.solve(self.pmodes[np.newaxis, np.newaxis], p.T[..., np.newaxis])[..., 0].T
+    return np.einsum("ik,k...->i...", self.pmodes, p)
+
+
+def diagnostics(pyqg):
+    """Every registered diagnostic of short runs that accumulate each step
+    (tavestart = 0, taveint = dt; pyqg/model.py:802-814), as time averages
+    (get_diagnostic) with their sample counts.  The layered model's modal
+    diagnostics need the numpy-1 reading of ``modal_projection``."""
+    pyqg.Model.modal_projection = _numpy1_modal_projection
+    c1 = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+              U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
+    lay = dict(nz=3, nx=32, H=[500., 1000., 2500.], U=[0.05, 0.02, 0.0],
+               V=[0., 0., 0.], rek=5.787e-7, dt=7200.0)
+    cases = {
+        "diag_qg_nx64.npz": (pyqg.QGModel, c1, {}, 11, 6),
+        "diag_layered_nz3_nx32.npz": (pyqg.LayeredModel, lay, {}, 12, 6),
+        "diag_qg_smag_nx32.npz": (pyqg.QGModel, dict(c1, nx=32),
+                                  dict(uv_parameterization=pyqg.Smagorinsky()), 13, 5),
+        "diag_qg_back_nx32.npz": (pyqg.QGModel, dict(c1, nx=32),
+                                  dict(q_parameterization=pyqg.BackscatterBiharmonic()), 14, 5),
+    }
+    out = {}
+    for name, (cls, kw, hooks, seed, nsteps) in cases.items():
+        m = cls(**kw, **hooks, tavestart=0.0, taveint=kw["dt"], log_level=0)
+        m.q = 1e-6 * np.random.default_rng(seed).standard_normal((m.nz, m.ny, m.nx))
+        q0 = np.asarray(m.q).copy()
+        for _ in range(nsteps):
+            m._step_forward()
+        rec = dict(q0=q0, nsteps=np.int64(nsteps), q=np.asarray(m.q).copy())
+        names = []
+        for n, d in m.diagnostics.items():
+            if not d["active"]:
+                continue
+            rec["diag_" + n] = np.asarray(m.get_diagnostic(n))
+            rec["count_" + n] = np.int64(d["count"])
+            names.append(n)
+        rec["names"] = np.array(names)
+        out[name] = rec
+    return out
 
 
 if __name__ == "__main__":
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
-        main()
+        main(sys.argv[1:] or None)

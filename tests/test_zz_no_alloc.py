@@ -61,6 +61,25 @@ def test_noalloc_rfft2_matches_plan_rfft2_on_consecutive_calls():
         assert rel_l2(got.cpu().numpy(), np.fft.rfftn(x.cpu().numpy(), axes=(-2, -1))) < TOL
 
 
+def test_noalloc_rfft2_rectangular_and_largest_grids():
+    """nx != ny (the x and y twiddle tables are sized and reloaded apart),
+    and the largest transform lengths: nx/2 = 2048 fills the x table and
+    ny = 2048 the y table, each with the scratch close to full."""
+    import torch
+    from pyqg_gb300 import _lib
+    L = _lib.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    rng = np.random.default_rng(12)
+    for (nz, ny, nx) in [(1, 64, 128), (2, 128, 64), (1, 250, 4096), (1, 2048, 480), (1, 64, 128)]:
+        assert nz * ny * (nx // 2 + 1) <= _lib.PQG_NOALLOC_MAX_COMPLEX
+        x = torch.from_numpy(rng.standard_normal((nz, ny, nx))).to(dev)
+        got = _noalloc_rfft2(L, x, ny, nx, stream)
+        want = _plan_rfft2(L, x, nz, ny, nx, stream)
+        assert rel_l2(got.cpu().numpy(), want.cpu().numpy()) < TOL
+        assert rel_l2(got.cpu().numpy(), np.fft.rfftn(x.cpu().numpy(), axes=(-2, -1))) < TOL
+
+
 def test_noalloc_rfft2_refuses_oversized_request():
     import torch
     from pyqg_gb300 import _lib
@@ -71,5 +90,11 @@ def test_noalloc_rfft2_refuses_oversized_request():
     x = torch.zeros((nplanes, n, n), dtype=torch.float64, device=dev)
     out = torch.empty((nplanes, n, n // 2 + 1), dtype=torch.complex128, device=dev)
     rc = L.pqg_rfft2_noalloc(x.data_ptr(), out.data_ptr(), nplanes, n, n, None)
+    assert rc == _lib.PQG_ERR_UNSUPPORTED
+    assert b"exceeds the static scratch" in L.pqg_last_error()
+    # the largest lengths together: 2048 * 2049 complex values, refused
+    x = torch.zeros((1, 2048, 4096), dtype=torch.float64, device=dev)
+    out = torch.empty((1, 2048, 2049), dtype=torch.complex128, device=dev)
+    rc = L.pqg_rfft2_noalloc(x.data_ptr(), out.data_ptr(), 1, 2048, 4096, None)
     assert rc == _lib.PQG_ERR_UNSUPPORTED
     assert b"exceeds the static scratch" in L.pqg_last_error()
