@@ -221,6 +221,15 @@ int pqg_ens_set_closure(pqg_ens *ens, pqg_cnn *net);
 int pqg_ens_state(pqg_ens *ens, void **q, void **qh, long long *tc,
                   double *t);
 
+/* Non-finite state flag (no counterpart in the reference, whose status
+ * output finds a NaN state only through its CFL assertion,
+ * pyqg/model.py:564-574).  The step kernels set it when a new spectral PV
+ * value is Inf or NaN; it lives in host-mapped memory, so pqg_nonfinite
+ * reads it without synchronizing: it reflects the kernels that have
+ * completed.  pqg_clear_nonfinite resets it (between kernels). */
+int pqg_nonfinite(const pqg_plan *plan, int *flag);
+int pqg_clear_nonfinite(pqg_plan *plan);
+
 /* Instrumentation for the profile / bench tooling (no counterpart in the
  * reference): `nsteps` fused steps like pqg_step but launched one by one
  * (no graph) with CUDA events around each kernel.  On return ms[0] / ms[1]
@@ -343,6 +352,17 @@ int pqg_cnn_adam(pqg_cnn *net, float lr, float beta1, float beta2, float eps,
 /* backward + Adam (beta1 0.9, beta2 0.999, eps 1e-8) */
 int pqg_cnn_train_step(pqg_cnn *net, const float *x, const float *t,
                        int batch, float lr, float *loss, void *stream);
+/* Pipeline status: synchronizes `stream` and returns PQG_ERR_TIMEOUT if a
+ * bounded wait of the network's tensor-core pipelines gave up since the
+ * last check (forward calls are asynchronous and do not check). */
+int pqg_cnn_status(pqg_cnn *net, void *stream);
+/* Failure tests (no counterpart in the reference): from pipeline unit
+ * `stop_unit` on (< 0: never) the producer of the halo-tile convolutions
+ * issues no more copies, so the other warps' bounded waits run out after
+ * `wait_ns` (0: one second); the kernel then waits (bounded) for its own
+ * MMAs and copies in flight, frees its tensor memory and returns, and the
+ * error is reported by pqg_cnn_status. */
+int pqg_cnn_set_fault(pqg_cnn *net, int stop_unit, unsigned long long wait_ns);
 
 #ifdef __cplusplus
 }

@@ -74,6 +74,8 @@ SIGNATURES = {
     "pqg_step_profile": (_I, [_P, ctypes.POINTER(State), _I,
                               ctypes.POINTER(_D), ctypes.POINTER(_I), _P]),
     "pqg_rfft2_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
+    "pqg_nonfinite": (_I, [_P, ctypes.POINTER(_I)]),
+    "pqg_clear_nonfinite": (_I, [_P]),
     "pqg_ens_last_error": (ctypes.c_char_p, []),
     "pqg_ens_create": (_I, [ctypes.POINTER(_P), _I, _I, _I, _I, _I]),
     "pqg_ens_destroy": (_I, [_P]),
@@ -105,6 +107,8 @@ SIGNATURES = {
     "pqg_cnn_adam": (_I, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                           ctypes.c_float, _P]),
     "pqg_cnn_train_step": (_I, [_P, _P, _P, _I, ctypes.c_float, _P, _P]),
+    "pqg_cnn_status": (_I, [_P, _P]),
+    "pqg_cnn_set_fault": (_I, [_P, _I, ctypes.c_ulonglong]),
 }
 
 _lock = threading.Lock()

@@ -262,6 +262,8 @@ struct HaloArgs {
   Img g;
   Epi e;
   int* err;
+  int stop_unit;         // >= 0: the producer issues no copy from this pipeline unit on (failure tests)
+  unsigned long long wait_ns;   // bound of every pipeline wait
 };
 
 template <int SX, int KS, int KUM>
@@ -316,12 +318,14 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
       // producer
       long long wq = 0;
       int u = 0;   // pipeline unit: (tile, channel unit)
-      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+      bool stopped = false;
+      for (int tile = blockIdx.x; tile < a.ntiles && ok && !stopped; tile += gridDim.x) {
         const int b = tile / per_img, r = tile - b * per_img;
         const int y0 = (r / a.tiles_x) * TY, x0 = (r % a.tiles_x) * 8 * SX;
         for (int h = 0; h < CH && ok; h++, u++) {
           const int hs = u % NH;
-          if (u >= NH) ok = tc::mbar_wait(&hempty[hs], ((u - NH) / NH) & 1);
+          if (u == a.stop_unit) { stopped = true; break; }
+          if (u >= NH) ok = tc::mbar_wait(&hempty[hs], ((u - NH) / NH) & 1, a.wait_ns);
           if (!ok) break;
           tc::mbar_expect_tx(&hfull[hs], hbytes);
           for (int gq = 0; gq < groups; gq++)
@@ -336,7 +340,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
           } else {
             for (int t = 0; t < NTAP && ok; t++, wq++) {
               const int ws = (int)(wq % NST);
-              if (wq >= NST) ok = tc::mbar_wait(&wempty[ws], (int)(((wq - NST) / NST) & 1));
+              if (wq >= NST) ok = tc::mbar_wait(&wempty[ws], (int)(((wq - NST) / NST) & 1), a.wait_ns);
               if (!ok) break;
               tc::mbar_expect_tx(&wfull[ws], wbytes);
               tc::bulk_load(wst + (size_t)ws * wbytes, a.wpk + (size_t)(t * CH + h) * N * cu, wbytes, &wfull[ws]);
@@ -363,8 +367,8 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
         const uint32_t acc = tmem + as * acc_cols + sx * N;
         for (int h = 0; h < CH && ok; h++, u++) {
           const int hs = u % NH;
-          ok = tc::mbar_wait(&hfull[hs], (u / NH) & 1);
-          if (ok && h == 0 && it >= 2) ok = tc::mbar_wait(&aempty[as], ((it - 2) >> 1) & 1);
+          ok = tc::mbar_wait(&hfull[hs], (u / NH) & 1, a.wait_ns);
+          if (ok && h == 0 && it >= 2) ok = tc::mbar_wait(&aempty[as], ((it - 2) >> 1) & 1, a.wait_ns);
           if (!ok) break;
           tc::fence_after();
           const uint64_t adh = ad0 + (uint64_t)hs * (hbytes >> 4);
@@ -373,7 +377,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
             const int ws = resident ? t * CH + h : (int)(wq % NST);
             // resident weights: waited for (and fenced) on the first tile only
             if (!resident || it == 0) {
-              ok = tc::mbar_wait(&wfull[ws], resident ? 0 : (int)((wq / NST) & 1));
+              ok = tc::mbar_wait(&wfull[ws], resident ? 0 : (int)((wq / NST) & 1), a.wait_ns);
               if (!ok) break;
               tc::fence_after();
             }
@@ -403,7 +407,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
     int it = 0;
     for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, it++) {
       const int as = it & 1;
-      const bool got = __all_sync(0xffffffffu, tc::mbar_wait(&afull[as], (it >> 1) & 1));
+      const bool got = __all_sync(0xffffffffu, tc::mbar_wait(&afull[as], (it >> 1) & 1, a.wait_ns));
       if (!got) { ok = false; break; }
       tc::fence_after();
       const int b = tile / per_img, r = tile - b * per_img;
@@ -1236,6 +1240,8 @@ struct pqg_cnn {
   float* loss = nullptr;
   int* err = nullptr;
   long long adam_t = 0;
+  int stop_unit = -1;                          // failure tests (pqg_cnn_set_fault)
+  unsigned long long wait_ns = 1000000000ull;  // bound of the halo-tile kernel's pipeline waits
 };
 
 namespace {
@@ -1451,6 +1457,8 @@ int launch_conv(pqg_cnn* net, const CnnLayer& l, bool dgrad, const bf16* in, int
     a.g = net->g;
     a.e = e;
     a.err = net->err;
+    a.stop_unit = net->stop_unit;
+    a.wait_ns = net->wait_ns;
     const dim3 grid(std::min(a.ntiles, net->nsm * (c.cps ? c.cps : net->cps)));
     auto fn = halo_kernel(c.sx, c.kin / 16, c.cu);
     if (!fn) return cfail(PQG_ERR_UNSUPPORTED, "no convolution kernel for this channel count");
@@ -1765,6 +1773,25 @@ PQG_API int pqg_cnn_set_norm(pqg_cnn* net, const float* in_mean, const float* in
 
 // y = net((x - in_mean) / in_std) * out_std + out_mean; x (batch, cin, H, W)
 // and y (batch, cout, H, W) are device arrays, FP32 or FP64.
+// Failure tests: from pipeline unit `stop_unit` on (a unit is one tile and
+// input-channel block of a CTA; < 0: never) the producer of the halo-tile
+// convolutions issues no more copies, so the other warps' waits run out
+// after `wait_ns` nanoseconds (0: the default of one second) and the kernel
+// takes its failure path.
+PQG_API int pqg_cnn_set_fault(pqg_cnn* net, int stop_unit, unsigned long long wait_ns) {
+  if (!net) return cfail(PQG_ERR_INVALID, "NULL network");
+  net->stop_unit = stop_unit;
+  net->wait_ns = wait_ns ? wait_ns : 1000000000ull;
+  return PQG_OK;
+}
+
+// Synchronizes `stream`; PQG_ERR_TIMEOUT if a pipeline wait of the
+// network's kernels gave up since the last check (the flag is cleared).
+PQG_API int pqg_cnn_status(pqg_cnn* net, void* stream) {
+  if (!net) return cfail(PQG_ERR_INVALID, "NULL network");
+  return check_err(net, (cudaStream_t)stream);
+}
+
 PQG_API int pqg_cnn_forward(pqg_cnn* net, const void* x, int x_f64, void* y, int y_f64, int batch, void* stream) {
   if (!net || !x || !y) return cfail(PQG_ERR_INVALID, "NULL argument");
   if (batch < 1 || batch > net->maxB) return cfail(PQG_ERR_INVALID, "bad batch size");

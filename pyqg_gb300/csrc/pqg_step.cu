@@ -75,7 +75,14 @@ struct Consts {
   const double* Ubg;    // (nz)
   const double* filtr;  // (nl, nk)
   double rek;
+  int* nonfinite;       // host-mapped flag, set when a new qh value is Inf or NaN
 };
+
+// Sets the plan's non-finite flag (host-mapped memory: the host reads it
+// without synchronizing) when a new spectral PV value is Inf or NaN.
+__device__ __forceinline__ void flag_nonfinite(int* nf, double2 v) {
+  if (nf && !(isfinite(v.x) && isfinite(v.y))) *reinterpret_cast<volatile int*>(nf) = 1;
+}
 
 // load a twiddle table into shared memory
 __device__ __forceinline__ void load_tw(double2* s, const double2* __restrict__ g, int n) {
@@ -391,6 +398,7 @@ __global__ void k_col_ab3(Geo g, Consts c, double2* qh,
     const size_t o = cidx(z, l, k, ny, nk);
     const double2 d = dq[o], p = dqp[o], pp = dqpp[o];
     const double2 qn = ab_update(c.filtr[(size_t)l * nk + k], qh[o], d, p, pp, c1, c2, c3);
+    flag_nonfinite(c.nonfinite, qn);
     qh[o] = qn;
     if (rotate) {
       dqpp[o] = p;
@@ -556,6 +564,7 @@ __global__ void k_col_fused(Geo g, Consts c, FusedColArgs A) {
     if (A.forcing) d = cadd(d, A.forcing[o]);
     const double2 pv = A.dqp[o], ppv = A.dqpp[o];
     const double2 qn = ab_update(c.filtr[(size_t)l * nk + k], bQO[l], d, pv, ppv, A.c1, A.c2, A.c3);
+    flag_nonfinite(c.nonfinite, qn);
     A.qh[o] = qn;
     A.dqout[o] = d;
     bQN[l] = qn;
@@ -855,6 +864,7 @@ __global__ void k_col_fused_fx(Geo g, Consts c, FusedColArgs A, const longlong2*
     if (A.forcing) d = cadd(d, A.forcing[o]);
     const double2 pv = A.dqp[o], ppv = A.dqpp[o];
     const double2 qn = ab_update(c.filtr[(size_t)l * nk + k], bQO[l], d, pv, ppv, A.c1, A.c2, A.c3);
+    flag_nonfinite(c.nonfinite, qn);
     A.qh[o] = qn;
     A.dqout[o] = d;
     bQN[l] = qn;
@@ -918,6 +928,8 @@ struct pqg_plan {
   int T_row = 128, rb = 1, T_col = 256;
   int T_row_batch = 128, rb_batch = 1;
   cudaStream_t cap_stream = nullptr;
+  int* nf_host = nullptr;      // non-finite flag (pinned, mapped) and its device address
+  int* nf_dev = nullptr;
   std::vector<GraphEntry> graphs;
   bool use_graphs = true;
 };
@@ -1024,6 +1036,7 @@ static Consts consts(const pqg_plan* p) {
   Consts c;
   c.a = p->a; c.kk = p->kk; c.ll = p->ll; c.k2l2 = p->k2l2; c.kQy = p->kQy;
   c.Ubg = p->Ubg; c.filtr = p->filtr; c.rek = p->rek;
+  c.nonfinite = p->nf_dev;
   return c;
 }
 
@@ -1441,8 +1454,26 @@ PQG_API int pqg_plan_create(pqg_plan** out, int nz, int ny, int nx) {
     pqg_plan_destroy(p);
     return fail(PQG_ERR_CUDA, "cudaStreamCreate failed");
   }
+  if (cudaHostAlloc((void**)&p->nf_host, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&p->nf_dev, p->nf_host, 0) != cudaSuccess) {
+    pqg_plan_destroy(p);
+    return fail(PQG_ERR_NOMEM, "mapped host flag allocation failed");
+  }
+  *p->nf_host = 0;
   PQG_CUDA(cudaDeviceSynchronize());
   *out = p;
+  return PQG_OK;
+}
+
+PQG_API int pqg_nonfinite(const pqg_plan* p, int* flag) {
+  if (!p || !flag) return fail(PQG_ERR_INVALID, "NULL argument to pqg_nonfinite");
+  *flag = *reinterpret_cast<volatile const int*>(p->nf_host);
+  return PQG_OK;
+}
+
+PQG_API int pqg_clear_nonfinite(pqg_plan* p) {
+  if (!p) return fail(PQG_ERR_INVALID, "NULL plan");
+  *reinterpret_cast<volatile int*>(p->nf_host) = 0;
   return PQG_OK;
 }
 
@@ -1454,6 +1485,7 @@ PQG_API int pqg_plan_destroy(pqg_plan* p) {
   cudaFree(p->filtr); cudaFree(p->scratch); cudaFree(p->twx_q); cudaFree(p->twy_q);
   cudaFree(p->work);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  if (p->nf_host) cudaFreeHost(p->nf_host);
   delete p;
   return PQG_OK;
 }

@@ -627,6 +627,21 @@ class PseudoSpectralKernel:
         if str(st["engine"]) != self._engine:
             self.engine = str(st["engine"])
 
+    # -- non-finite state ------------------------------------------------
+    @property
+    def nonfinite(self):
+        """True once a step has produced an Inf or NaN spectral PV value.
+        The step kernels set the flag in host-mapped memory, so reading it
+        does not synchronize: it covers the steps that have completed."""
+        flag = ctypes.c_int(0)
+        _lib.check(self._L.pqg_nonfinite(self._plan, ctypes.byref(flag)))
+        return bool(flag.value)
+
+    def clear_nonfinite(self):
+        """Reset the non-finite flag (waits for the queued steps first)."""
+        self._stream.synchronize()
+        _lib.check(self._L.pqg_clear_nonfinite(self._plan))
+
     # -- device views (no host copy): for GPU-side parameterizations -------
     def device_field(self, name):
         """The device tensor holding field `name` (read it, do not keep it

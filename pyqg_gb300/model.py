@@ -309,10 +309,15 @@ class Model(PseudoSpectralKernel):
             return tend if on_device else tend.cpu().numpy()
 
     def _print_status(self):
-        """Log KE and CFL every `twrite` steps; fail if CFL >= 1."""
+        """Log KE and CFL every `twrite` steps; fail if CFL >= 1.  A state
+        the step kernels flagged as non-finite gives CFL = NaN, so the
+        assertion fails as the reference's does for a NaN velocity, without
+        downloading the velocity fields."""
         if self.log_level and (self.tc % self.twrite) == 0:
+            self._stream.synchronize()
+            nonfinite = self.nonfinite
             self.ke = self._calc_ke()
-            self.cfl = self._calc_cfl()
+            self.cfl = float("nan") if nonfinite else self._calc_cfl()
             self.logger.info('Step: %i, Time: %3.2e, KE: %3.2e, CFL: %4.3f',
                              self.tc, self.t, self.ke, self.cfl)
             assert self.cfl < 1., self.logger.error('CFL condition violated')

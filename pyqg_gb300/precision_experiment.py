@@ -74,7 +74,8 @@ def run(members=8, spinup_years=5.0, years=2.0, sample_every=240, seed0=2000, lo
     f64, f32 = flux["fp64"] / cnt, flux["fp32"] / cnt
     rep = {
         "config": dict(members=members, nx=nx, dt=dt, spinup_years=spinup_years, years=years,
-                       samples=cnt, seed0=seed0),
+                       samples=cnt, seed0=seed0,
+                       model_steps=int(round(spinup_years * YEAR / dt)) + 10 + n),
         "ten_step_rel_l2_q": err10,
         "ke_spectrum": dict(max_rel_diff_energy_containing=float(rel[energetic].max()),
                             mean_rel_diff_energy_containing=float(rel[energetic].mean()),

@@ -309,3 +309,38 @@ def test_row_tile_and_halo_kernels_agree(channels, batch, monkeypatch):
         for g in gs[1:]:
             assert rel_l2(gs[0][ws], g[ws]) < 2e-2
             assert rel_l2(gs[0][bs], g[bs]) < 2e-2
+
+
+def test_pipeline_timeout_reports_and_recovers(monkeypatch):
+    """The failure path of the halo-tile convolution, made to run without a
+    GPU fault: the producer stops issuing copies from pipeline unit 1 on,
+    so the MMA issuers' and epilogue warps' bounded waits (2 ms here) run
+    out.  The kernel waits for its own MMAs and copies in flight, frees its
+    tensor memory and returns; pqg_cnn_status reports PQG_ERR_TIMEOUT once,
+    and the next forward is bit-identical to one taken before the fault."""
+    import ctypes
+    import torch
+    from pyqg_gb300 import _lib
+    from pyqg_gb300.closure import ConvNet
+    monkeypatch.setenv("PQG_CNN_ROWS", "0")      # halo-tile kernel on every layer it takes
+    channels = (2, 128, 64, 32, 2)
+    batch = 48                                    # several tiles per persistent CTA
+    net = ConvNet(channels, max_batch=batch, seed=21)
+    L = _lib.lib()
+    h = net._h
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    x = torch.from_numpy(np.random.default_rng(21).standard_normal((batch, 2, 64, 64)).astype(np.float32)).cuda()
+    y0 = net.forward(x).cpu().numpy()
+    assert L.pqg_cnn_status(h, st) == _lib.PQG_OK
+    _lib.check(L.pqg_cnn_set_fault(h, 1, 2000000))
+    net.forward(x)
+    rc = L.pqg_cnn_status(h, st)
+    assert rc == _lib.PQG_ERR_TIMEOUT
+    assert b"timed out" in L.pqg_cnn_last_error()
+    assert L.pqg_cnn_status(h, st) == _lib.PQG_OK          # reported once
+    _lib.check(L.pqg_cnn_set_fault(h, -1, 0))
+    y1 = net.forward(x).cpu().numpy()
+    assert L.pqg_cnn_status(h, st) == _lib.PQG_OK
+    np.testing.assert_array_equal(y1, y0)
+    ref = _torch_net(channels, net.params, net.layer_slices(), x).cpu().numpy()
+    assert rel_l2(y1, ref) < 1e-2

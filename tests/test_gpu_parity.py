@@ -288,3 +288,37 @@ def test_non_square_kernel_vs_oracle(P, nx, ny, engines):
         f._step_fused(30)
         assert rel_l2(s.q, o.q) < TOL_100, engine
         np.testing.assert_array_equal(f.q, s.q)
+
+
+@pytest.mark.parametrize("engine", ["fixed", "fp64"])
+def test_nonfinite_flag_and_status_assertion(engine, quiet):
+    """A NaN placed in q on the host is caught by the step kernels' flag,
+    read without synchronizing; with status output on, the CFL assertion
+    fails as the reference's does for a NaN state (pyqg/model.py:564-574)."""
+    import pyqg_gb300 as P
+    q = 1e-7 * np.random.default_rng(17).standard_normal((2, 32, 32))
+    m = P.QGModel(nx=32, dt=7200.0, tmax=4 * 7200.0, **quiet)
+    m.engine = engine
+    m.q = q
+    m.run()
+    torch_sync()
+    assert not m.nonfinite
+    bad = q.copy()
+    bad[1, 3, 5] = np.nan
+    m.q = bad
+    m.tmax = m.t + 3 * 7200.0
+    m.run()
+    torch_sync()
+    assert m.nonfinite
+    m.clear_nonfinite()
+    assert not m.nonfinite
+    loud = P.QGModel(nx=32, dt=7200.0, twrite=1, log_level=1, tavestart=1e30, taveint=1e30)
+    loud.engine = engine
+    loud.q = bad
+    with pytest.raises(AssertionError):
+        loud._step_forward()
+
+
+def torch_sync():
+    import torch
+    torch.cuda.synchronize()
