@@ -257,6 +257,21 @@ int pqg_step_profile(pqg_plan *plan, pqg_state *state, int nsteps,
 int pqg_rfft2_noalloc(const double *x, double *xh, int nplanes, int ny,
                       int nx, void *stream);
 
+/* Inversion matrices built in FP64 on the device (the benchmark spec's
+ * precision form builds its matrices here and rounds them once):
+ * a (nz, nz, nl, nk) = (S - kappa^2 I)^-1 per wavenumber, kappa^2 =
+ * kk[k]^2 + ll[l]^2, 0 where singular (kappa = 0).  S is a HOST nz x nz
+ * row-major array; kk (nk), ll (nl) and a are DEVICE arrays.
+ *   form 0: two-layer QG, F1 = S[0][1], F2 = S[1][0]
+ *           (replaces QGModel._initialize_inversion_matrix,
+ *           pyqg/qg_model.py:146-161), bit-identical to the host build;
+ *   form 1: layered, nz = 2..8 (replaces LayeredModel.
+ *           _initialize_inversion_matrix, pyqg/layered_model.py:211-229);
+ *           nz = 2 bit-identical, nz > 2 by Gauss-Jordan elimination. */
+int pqg_inversion_matrix(int form, int nz, int nl, int nk, const double *S,
+                         const double *kk, const double *ll, double *a,
+                         void *stream);
+
 /* Spectral advective tendency of nplanes physical fields f by (u, v):
  * out_h = ik fft(u f) + il fft(v f), FP64 transforms
  * (replaces Model._advect, pyqg/model.py:539-558). */

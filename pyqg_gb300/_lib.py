@@ -91,6 +91,7 @@ SIGNATURES = {
     "pqg_ens_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
                            ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_D)]),
     "pqg_advect": (_I, [_P, _P, _P, _P, _I, _P, _P]),
+    "pqg_inversion_matrix": (_I, [_I, _I, _I, _I, _P, _P, _P, _P, _P]),
     "pqg_diag_accumulate": (_I, [_P, _I, ctypes.POINTER(DiagFields), _P, _P]),
     "pqg_coarse_forcing": (_I, [_P, _P, _P, _P, _P, _P]),
     "pqg_cnn_last_error": (ctypes.c_char_p, []),

@@ -1851,6 +1851,103 @@ PQG_API int pqg_step_profile(pqg_plan* p, pqg_state* s, int nsteps, double* ms, 
 }
 
 // ---------------------------------------------------------------------------
+// Inversion matrices in FP64 on the device (the precision form builds its
+// matrices here before rounding them once): a = (S - kappa^2 I)^-1 per
+// wavenumber, kappa^2 = kk[k]^2 + ll[l]^2, the singular kappa = 0 entry 0.
+//   form 0: two-layer QG closed form (pyqg/qg_model.py:146-161) from
+//           F1 = S[0][1], F2 = S[1][0]: det = kappa^2 (kappa^2 + F1 + F2)
+//   form 1: layered (pyqg/layered_model.py:211-229): the nz = 2 closed form
+//           det = (S00 - kappa^2)(S11 - kappa^2) - S01 S10, Gauss-Jordan
+//           elimination with partial pivoting for nz > 2
+// The closed forms follow numpy's operation order without contraction, so
+// they equal the host build bit for bit; nz > 2 differs from LAPACK's LU in
+// the last bits.
+// ---------------------------------------------------------------------------
+struct InvArgs {
+  int nz, nl, nk, form;
+  double S[PQG_DIAG_MAXZ * PQG_DIAG_MAXZ];
+};
+
+__global__ void k_inversion(InvArgs A, const double* __restrict__ kk, const double* __restrict__ ll, double* a) {
+  const int n = A.nl * A.nk;
+  const int nz = A.nz;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int l = i / A.nk, k = i - l * A.nk;
+    const double w = __dadd_rn(__dmul_rn(kk[k], kk[k]), __dmul_rn(ll[l], ll[l]));
+    auto put = [&](int r, int c, double v) { a[((size_t)(r * nz + c) * A.nl + l) * A.nk + k] = v; };
+    if (nz == 2) {
+      double det;
+      if (A.form == 0) {
+        const double F1 = A.S[1], F2 = A.S[2];
+        det = __dmul_rn(w, __dadd_rn(__dadd_rn(w, F1), F2));
+      } else {
+        det = __dsub_rn(__dmul_rn(__dsub_rn(A.S[0], w), __dsub_rn(A.S[3], w)), __dmul_rn(A.S[1], A.S[2]));
+      }
+      if (det == 0.0 || !isfinite(det)) {
+        put(0, 0, 0.0); put(0, 1, 0.0); put(1, 0, 0.0); put(1, 1, 0.0);
+        continue;
+      }
+      const double di = __drcp_rn(det);
+      if (A.form == 0) {
+        const double F1 = A.S[1], F2 = A.S[2];
+        put(0, 0, __dmul_rn(-__dadd_rn(w, F2), di));
+        put(0, 1, __dmul_rn(-F1, di));
+        put(1, 0, __dmul_rn(-F2, di));
+        put(1, 1, __dmul_rn(-__dadd_rn(w, F1), di));
+      } else {
+        put(0, 0, __dmul_rn(__dsub_rn(A.S[3], w), di));
+        put(0, 1, __dmul_rn(-A.S[1], di));
+        put(1, 0, __dmul_rn(-A.S[2], di));
+        put(1, 1, __dmul_rn(__dsub_rn(A.S[0], w), di));
+      }
+      continue;
+    }
+    double m[PQG_DIAG_MAXZ][2 * PQG_DIAG_MAXZ];
+    bool singular = (l == 0 && k == 0);
+    for (int r = 0; r < nz; r++)
+      for (int c = 0; c < 2 * nz; c++)
+        m[r][c] = c < nz ? (r == c ? __dsub_rn(A.S[r * nz + c], w) : A.S[r * nz + c]) : (c - nz == r ? 1.0 : 0.0);
+    for (int c = 0; c < nz && !singular; c++) {
+      int piv = c;
+      for (int r = c + 1; r < nz; r++)
+        if (fabs(m[r][c]) > fabs(m[piv][c])) piv = r;
+      if (m[piv][c] == 0.0) { singular = true; break; }
+      if (piv != c)
+        for (int q = 0; q < 2 * nz; q++) { const double t = m[c][q]; m[c][q] = m[piv][q]; m[piv][q] = t; }
+      const double inv = 1.0 / m[c][c];
+      for (int q = 0; q < 2 * nz; q++) m[c][q] *= inv;
+      for (int r = 0; r < nz; r++) {
+        if (r == c) continue;
+        const double f = m[r][c];
+        if (f != 0.0)
+          for (int q = 0; q < 2 * nz; q++) m[r][q] = __fma_rn(-f, m[c][q], m[r][q]);
+      }
+    }
+    for (int r = 0; r < nz; r++)
+      for (int c = 0; c < nz; c++) {
+        const double v = m[r][nz + c];
+        put(r, c, (singular || !isfinite(v)) ? 0.0 : v);
+      }
+  }
+}
+
+PQG_API int pqg_inversion_matrix(int form, int nz, int nl, int nk, const double* S, const double* kk,
+                                 const double* ll, double* a, void* stream) {
+  if (!S || !kk || !ll || !a || nl < 1 || nk < 1) return fail(PQG_ERR_INVALID, "bad argument to pqg_inversion_matrix");
+  if (nz < 2 || nz > PQG_DIAG_MAXZ) return fail(PQG_ERR_UNSUPPORTED, "nz must be 2..8");
+  if (form != 0 && form != 1) return fail(PQG_ERR_INVALID, "form must be 0 (two-layer QG) or 1 (layered)");
+  if (form == 0 && nz != 2) return fail(PQG_ERR_INVALID, "the two-layer QG form needs nz = 2");
+  InvArgs A{};
+  A.nz = nz; A.nl = nl; A.nk = nk; A.form = form;
+  for (int i = 0; i < nz * nz; i++) A.S[i] = S[i];
+  const size_t n = (size_t)nl * nk;
+  const unsigned grid = (unsigned)std::min<size_t>((n + 127) / 128, 152 * 16);
+  k_inversion<<<grid, 128, 0, (cudaStream_t)stream>>>(A, kk, ll, a);
+  PQG_CUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Forward 2-D real transform that allocates no device memory.
 //
 // For callers that cannot call cudaMalloc: processes whose device memory is

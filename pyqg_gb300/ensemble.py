@@ -24,8 +24,45 @@ from .qg_model import qg_inversion_matrix
 YEAR = 360 * 86400.0
 
 
-def _member_constants(kind, kw):
-    """FP64 constants of one member: (nz, nx, a, kk, ll, filtr, Ubg, Qy, rek)."""
+_device_matrices = {}
+
+
+def device_inversion_matrix(S, kk, ll, two_layer_qg=False):
+    """The FP64 inversion matrix a (nz, nz, nl, nk) = (S - kappa^2 I)^-1,
+    built on the GPU (``pqg_inversion_matrix``), as a host array.  With
+    ``two_layer_qg`` the two-layer QG closed form with F1 = S[0, 1],
+    F2 = S[1, 0] (``pyqg/qg_model.py:146-161``), else the layered form
+    (``pyqg/layered_model.py:211-229``).  Results are cached per input."""
+    import torch
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    kk = np.ascontiguousarray(kk, dtype=np.float64)
+    ll = np.ascontiguousarray(ll, dtype=np.float64)
+    key = (bool(two_layer_qg), S.tobytes(), kk.tobytes(), ll.tobytes())
+    hit = _device_matrices.get(key)
+    if hit is not None:
+        return hit
+    L = _lib.lib()
+    nz, nl, nk = S.shape[0], ll.size, kk.size
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    with torch.cuda.stream(stream):
+        kk_d = torch.from_numpy(kk).to(dev)
+        ll_d = torch.from_numpy(ll).to(dev)
+        a = torch.empty((nz, nz, nl, nk), dtype=torch.float64, device=dev)
+        _lib.check(L.pqg_inversion_matrix(0 if two_layer_qg else 1, nz, nl, nk, S.ctypes.data,
+                                          kk_d.data_ptr(), ll_d.data_ptr(), a.data_ptr(),
+                                          ctypes.c_void_p(stream.cuda_stream)))
+        out = a.cpu().numpy()
+    if len(_device_matrices) > 64:
+        _device_matrices.clear()
+    _device_matrices[key] = out
+    return out
+
+
+def _member_constants(kind, kw, device_matrices=False):
+    """FP64 constants of one member: (nz, nx, a, kk, ll, filtr, Ubg, Qy, rek).
+    With ``device_matrices`` the inversion matrix is built in FP64 on the
+    GPU (the precision form), else by the model classes' host code."""
     nx = kw.get("nx", 64)
     L = kw.get("L", 1e6)
     g = grid_constants(nx, nx, L, L)
@@ -37,7 +74,10 @@ def _member_constants(kind, kw):
         U1, U2 = kw.get("U1", 0.025), kw.get("U2", 0.0)
         F1 = rd ** -2 / (1. + delta)
         F2 = delta * F1
-        a = qg_inversion_matrix(g["wv2"], F1, F2)
+        if device_matrices:
+            a = device_inversion_matrix(np.array([[-F1, F1], [F2, -F2]]), g["kk"], g["ll"], True)
+        else:
+            a = qg_inversion_matrix(g["wv2"], F1, F2)
         Qy = np.array([beta + F1 * (U1 - U2), beta - F2 * (U1 - U2)])
         Ubg = np.array([U1, U2])
         nz = 2
@@ -50,7 +90,8 @@ def _member_constants(kind, kw):
         gg = kw.get("g", 9.81)
         gpi = gg * (rho[1:] - rho[:-1]) / rho[:-1]
         S = stretching_matrix(nz, f ** 2, H, gpi, kw.get("rd"), kw.get("delta"))
-        a = layered_inversion_matrix(S, g["wv2"])
+        a = (device_inversion_matrix(S, g["kk"], g["ll"]) if device_matrices
+             else layered_inversion_matrix(S, g["wv2"]))
         Qy = beta - S @ U
         Ubg = U
     else:
@@ -178,7 +219,10 @@ class Ensemble:
         if precision not in ("fp32", "fp64"):
             raise ValueError("precision must be 'fp32' or 'fp64'")
         self.precision = precision
-        consts = [_member_constants(kind, kw) for kind, kw in members]
+        # the FP32 form builds its inversion matrices in FP64 on the GPU and
+        # rounds them once; FP64 members keep the host build, so that they
+        # reproduce the single-model step bit for bit
+        consts = [_member_constants(kind, kw, device_matrices=precision == "fp32") for kind, kw in members]
         dts = [float(kw.get("dt", 7200.0)) for _, kw in members]
         keys = {}
         for i, c in enumerate(consts):

@@ -212,3 +212,38 @@ def test_member_kernel_fp64_equals_single_models(monkeypatch):
     monkeypatch.delenv("PQG_ENS_FUSED")
     tuned = ens.autotune()
     assert set(tuned[0]) >= {"member_kernel", "member_threads", "member_ms_4_steps"}
+
+
+def test_device_inversion_matrices_match_host_build():
+    """FP64 inversion matrices built on the GPU (pqg_inversion_matrix): the
+    two-layer closed forms bit for bit against the host build (the model
+    classes' code, which restates pyqg/qg_model.py:146-161 and
+    pyqg/layered_model.py:211-229), nz > 2 by Gauss-Jordan elimination
+    within 1e-14 of each wavenumber's largest entry, the singular
+    kappa = 0 entry 0."""
+    from pyqg_gb300.ensemble import device_inversion_matrix
+    from pyqg_gb300.layered_model import layered_inversion_matrix, stretching_matrix
+    from pyqg_gb300.model import grid_constants
+    from pyqg_gb300.qg_model import qg_inversion_matrix
+    for nx in (64, 256):
+        g = grid_constants(nx, nx, 1e6, 1e6)
+        F1 = 15000.0 ** -2 / 1.25
+        F2 = 0.25 * F1
+        host = qg_inversion_matrix(g["wv2"], F1, F2)
+        dev = device_inversion_matrix(np.array([[-F1, F1], [F2, -F2]]), g["kk"], g["ll"], True)
+        np.testing.assert_array_equal(dev, host)
+        f2, gg = 0.0001236812857687059 ** 2, 9.81
+        for nz, H in ((2, [500., 2000.]), (3, [500., 1000., 2500.]), (4, [300., 600., 1200., 2400.]),
+                      (8, [100., 150., 200., 300., 400., 500., 800., 1550.])):
+            rho = np.arange(nz) * 0.3 + 1025
+            gpi = gg * (rho[1:] - rho[:-1]) / rho[:-1]
+            S = stretching_matrix(nz, f2, np.array(H), gpi)
+            host = layered_inversion_matrix(S, g["wv2"])
+            dev = device_inversion_matrix(S, g["kk"], g["ll"])
+            assert np.all(dev[:, :, 0, 0] == 0)
+            if nz == 2:
+                np.testing.assert_array_equal(dev, host)
+            else:
+                scale = np.abs(host).max(axis=(0, 1))
+                scale[0, 0] = 1.0
+                assert (np.abs(dev - host).max(axis=(0, 1)) / scale).max() <= 1e-14, nz
