@@ -167,8 +167,9 @@ def _ref_kernel(mod, fft_workers):
 
 
 def cpu_model_steps(nsteps, nx=256, dt=3600.0, seed=0, threads=None, fft_workers=0):
-    """Run `nsteps` config-2 steps on the CPU with the reference's compiled
-    kernel (kind 'reference'; `threads` OpenMP threads for its loops,
+    """Run `nsteps` config-2 steps on the CPU with the reference itself
+    (kind 'reference': pyqg's unchanged QGModel and _step_forward over its
+    compiled kernel, `threads` OpenMP threads for the kernel's loops,
     `fft_workers` > 0 for multithreaded transforms) or the numpy oracle
     (kind 'port').  Returns (seconds, kind, cores)."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
@@ -190,18 +191,39 @@ def cpu_model_steps(nsteps, nx=256, dt=3600.0, seed=0, threads=None, fft_workers
         if not build_ref.available():
             build_ref.build(quiet=True)
         mod = build_ref.load()
-        k = _ref_kernel(mod, fft_workers)(2, nx, nx, threads, 0, 0)
-        k.ll = g["ll"]
-        k.kk = g["kk"]
-        k.a = a
-        k.Ubg = Ubg
-        k.Qy = Qy
-        k.filtr = filtr
-        k.rek = C2["rek"]
-        k.dt = dt
-        k.q = q0
-        step = lambda: (k._invert(), k._do_advection(), k._do_friction(), k._forward_timestep())
-        kind = "reference"
+        kernel_cls = _ref_kernel(mod, fft_workers)
+        try:
+            # the reference's own, unchanged QGModel over its compiled kernel:
+            # its set-up, its _step_forward (pyqg/model.py:406-436)
+            import types
+            import ref_import
+            kmod = types.ModuleType("pyqg_ref_kernel_threads")
+            kmod.PseudoSpectralKernel = kernel_cls
+            for name in ("tendency_forward_euler", "tendency_ab2", "tendency_ab3"):
+                setattr(kmod, name, getattr(mod, name))
+            ref = ref_import.import_reference_on(kmod)
+            import warnings
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                m = ref.QGModel(nx=nx, dt=dt, ntd=threads, **C2, **QUIET)
+            m.q = q0
+            step = m._step_forward
+            kind = "reference"
+        except ImportError:
+            # staged reference package absent: the compiled kernel's stages
+            # with the same constants
+            k = kernel_cls(2, nx, nx, threads, 0, 0)
+            k.ll = g["ll"]
+            k.kk = g["kk"]
+            k.a = a
+            k.Ubg = Ubg
+            k.Qy = Qy
+            k.filtr = filtr
+            k.rek = C2["rek"]
+            k.dt = dt
+            k.q = q0
+            step = lambda: (k._invert(), k._do_advection(), k._do_friction(), k._forward_timestep())
+            kind = "reference"
     except Exception:
         o = O.OracleKernel(2, nx, nx, a, g["kk"], g["ll"], Ubg, Qy, filtr, C2["rek"], dt)
         o.set_q(q0)
@@ -249,7 +271,8 @@ def cpu_baseline(dt, sample_steps):
     secs, kind, cores = cpu_model_steps(sample_steps, dt=dt, threads=th, fft_workers=fw)
     return {"value": sim_yr_per_hr(sample_steps, dt, secs), "unit": "sim-yr/hr",
             "cores": cores, "kind": kind,
-            "sample": "%d config-2 steps (nx=256, FP64) on the host, %.1f ms/step (%s, the fastest of "
+            "sample": "%d config-2 steps (nx=256, FP64) on the host through pyqg's own QGModel._step_forward "
+                      "over its compiled kernel, %.1f ms/step (%s, the fastest of "
                       "1 thread / all cores / multithreaded FFT)"
                       % (sample_steps, 1e3 * secs / sample_steps, cpu_variant_name(th, fw))}
 
@@ -276,7 +299,8 @@ def run_reference(args, rank, world):
                                    "%d model steps per timed step" % sample,
                        "model_steps_per_step": sample, "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": value, "unit": "sim-yr/hr", "cores": cores, "kind": kind,
-                             "sample": "%d x %d config-2 steps (%s)"
+                             "sample": "%d x %d config-2 steps through pyqg's own QGModel._step_forward "
+                                       "over its compiled kernel (%s)"
                                        % (args.steps, sample, cpu_variant_name(th, fw))},
             "e2e": {"value": value, "unit": "sim-yr/hr", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
