@@ -20,10 +20,11 @@ reference tree or Cython:
 ``cythonize``  needs the reference tree and Cython.  Writes
                ``oracle/_ref/pyqg_ref_kernel.c`` (generated C).
 ``stage``      needs the reference tree.  Copies the reference package's
-               Python modules (``pyqg/*.py``, not its tests or kernel) to
-               ``oracle/_ref/pyqg_src/pyqg/``, so that tests can run the
-               unchanged ``pyqg.Model`` classes over another kernel module on
-               a machine without the tree.
+               Python modules (``pyqg/*.py``, not its kernel) and its tests
+               (``pyqg/tests``) to ``oracle/_ref/pyqg_src/pyqg/``, so that
+               tests can run the unchanged ``pyqg.Model`` classes and the
+               reference's own test suite over another kernel module on a
+               machine without the tree.
 ``compile``    needs gcc, the Python headers and numpy.  Compiles that C file
                with ``-O3 -fopenmp`` (``setup.py:77-124`` of the reference uses
                ``-fopenmp`` the same way) into ``oracle/_ref/pyqg_ref_kernel*.so``.
@@ -90,6 +91,10 @@ def stage_python():
     for name in sorted(os.listdir(src)):
         if name.endswith(".py"):
             shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
+    # the reference's own tests and their fixtures (tests/reference_suite.py
+    # runs them over a chosen kernel module)
+    shutil.copytree(os.path.join(src, "tests"), os.path.join(dst, "tests"),
+                    ignore=shutil.ignore_patterns("__pycache__", "*.pyc"))
     return dst
 
 
