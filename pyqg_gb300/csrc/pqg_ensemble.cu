@@ -599,6 +599,8 @@ __global__ void e_energy(EGeo g, EConsts<typename Sc<V>::T> c, const V* qh, doub
   }
 }
 
+#include "pqg_ens_warp.cuh"
+
 }  // namespace
 
 // ===========================================================================
@@ -620,6 +622,8 @@ struct pqg_ens {
   int T_row = 128, rb = 1, T_col = 128, C = 1;
   bool fused = false;           // whole steps per CTA (e_member_steps; the autotuner's choice)
   int T_mem = 256;              // threads of the per-member kernel
+  int w_row = 8, w_col = 4;     // warps per CTA of the warp-owned FP32 row / column kernels
+  bool w_stage = true;          // the row kernel stages its planes' tiles (when its rows divide ny)
   int rb_mem = 16;              // its rows per chunk of the row transforms
   int nfield = 3;               // mixed planes per member: U, V, Q (+ forcing F)
   long long version = 0;        // bumped when launch parameters change (graph cache key)
@@ -847,6 +851,86 @@ EK<float2>::Member EK<float2>::member64() { return e_member_steps<float2, 6>; }
 template <>
 EK<double2>::Member EK<double2>::member64() { return nullptr; }
 
+// Warp-owned FP32 row and column kernels (pqg_ens_warp.cuh): FP32 groups
+// with 16 <= nx <= 256, 16 <= ny <= 256 and at most three layers.  Such a
+// group always runs them (not the per-member kernel), so that its results
+// do not depend on the launch choices; PQG_ENS_WARP=0 turns them off.
+bool warp_on(const pqg_ens* e) {
+  if (e->prec != 4 || e->nz > 3 || e->M < 8 || e->M > 128 || e->ny < 16 || e->ny > 256) return false;
+  if (const char* s = getenv("PQG_ENS_WARP"))
+    if (s[0] == '0') return false;
+  return true;
+}
+
+typedef void (*RowW)(EGeo, EConsts<float>, float2*, const float*, const float2*, float, float*);
+typedef void (*ColW)(EGeo, EConsts<float>, float2*, float2*, const float2*, float2*, const float2*, float, float,
+                     float, int);
+template <bool STAGE>
+RowW row_w_s(int M) {
+  switch (lg2(M)) {
+    case 3: return e_row_w<3, STAGE>;
+    case 4: return e_row_w<4, STAGE>;
+    case 5: return e_row_w<5, STAGE>;
+    case 6: return e_row_w<6, STAGE>;
+    case 7: return e_row_w<7, STAGE>;
+    default: return nullptr;
+  }
+}
+// the staged row kernel: when chosen and the CTA's rows (warps x 256 / M)
+// divide ny
+bool row_staged(const pqg_ens* e) { return e->w_stage && e->ny % (e->w_row * 256 / e->M) == 0; }
+template <int L>
+ColW col_w_nz(int nz) {
+  switch (nz) {
+    case 1: return e_col_w<L, 1>;
+    case 2: return e_col_w<L, 2>;
+    case 3: return e_col_w<L, 3>;
+    default: return nullptr;
+  }
+}
+ColW col_w(int N, int nz) {
+  switch (lg2(N)) {
+    case 4: return col_w_nz<4>(nz);
+    case 5: return col_w_nz<5>(nz);
+    case 6: return col_w_nz<6>(nz);
+    case 7: return col_w_nz<7>(nz);
+    case 8: return col_w_nz<8>(nz);
+    default: return nullptr;
+  }
+}
+
+int launch_row_w(pqg_ens* e, bool first, cudaStream_t st) {
+  const int G = e->M / 8, rpw = 32 / G, W = e->w_row;
+  const long long nrows = (long long)e->B * e->nz * e->ny, per = (long long)W * rpw;
+  const bool stage = row_staged(e);
+  const size_t smem = sizeof(float2) * ((size_t)e->nx + (size_t)W * rpw * wg::wstride(e->M) +
+                                        (stage ? (size_t)(e->M + 1) * (W * rpw + 1) : 0));
+  (stage ? row_w_s<true>(e->M) : row_w_s<false>(e->M))<<<(unsigned)((nrows + per - 1) / per), 32 * W, smem, st>>>(
+      egeo(e), econsts<float2>(e), (float2*)e->scratch, first ? (const float*)e->q : nullptr,
+      (const float2*)e->twx, (float)(1.0 / ((double)e->nx * e->ny)), e->net ? (float*)e->qcur : nullptr);
+  ECUDA(cudaGetLastError());
+  return PQG_OK;
+}
+
+int launch_col_w(pqg_ens* e, cudaStream_t st) {
+  double c1, c2, c3;
+  if (e->ablevel <= 0) { c1 = e->dt; c2 = 0.0; c3 = 0.0; }
+  else if (e->ablevel == 1) { c1 = 1.5 * e->dt; c2 = -0.5 * e->dt; c3 = 0.0; }
+  else { c1 = 23. / 12. * e->dt; c2 = -16. / 12. * e->dt; c3 = 5. / 12. * e->dt; }
+  const int G = e->ny / 8, upw = 32 / G, W = e->w_col;
+  const long long nunits = (long long)e->B * e->nk, per = (long long)W * upw;
+  const size_t smem = sizeof(float2) * ((size_t)e->ny + (size_t)W * upw * wg::wstride(e->ny));
+  col_w(e->ny, e->nz)<<<(unsigned)((nunits + per - 1) / per), 32 * W, smem, st>>>(
+      egeo(e), econsts<float2>(e), (float2*)e->scratch, (float2*)e->qh, (const float2*)e->dq[e->role_p],
+      (float2*)e->dq[e->role_pp], (const float2*)e->twy, (float)c1, (float)c2, (float)c3, e->net ? 1 : 0);
+  ECUDA(cudaGetLastError());
+  std::swap(e->role_p, e->role_pp);
+  e->ablevel = e->ablevel >= 2 ? 2 : e->ablevel + 1;
+  e->tc += 1;
+  e->t += e->dt;
+  return PQG_OK;
+}
+
 // per-member kernel: rows per chunk and shared memory; 0 when the group's
 // shape does not fit it (square, 16 <= nx <= 64, at most 4 layers, FP64
 // only up to nx = 32, shared memory within the 200 KB the kernels opt in to)
@@ -858,7 +942,7 @@ size_t member_smem(const pqg_ens* e) {
   return b <= 200 * 1024 ? b : 0;
 }
 bool member_on(const pqg_ens* e) {
-  if (e->net || !member_smem(e)) return false;
+  if (e->net || !member_smem(e) || warp_on(e)) return false;
   if (const char* env = getenv("PQG_ENS_FUSED")) {   // 1: always, 0: never
     if (env[0] == '1') return true;
     if (env[0] == '0') return false;
@@ -903,10 +987,11 @@ int launch_member(pqg_ens* e, int nsteps, cudaStream_t st) {
 template <class V>
 int step_two(pqg_ens* e, int nsteps, cudaStream_t st) {
   int rc = launch_prologue<V>(e, st);
+  const bool w = warp_on(e);
   for (int i = 0; i < nsteps && !rc; i++) {
-    rc = launch_row_adv<V>(e, i == 0, st);
+    rc = w ? launch_row_w(e, i == 0, st) : launch_row_adv<V>(e, i == 0, st);
     if (!rc && e->net) rc = launch_closure<V>(e, st);
-    if (!rc) rc = launch_col_fused<V>(e, st);
+    if (!rc) rc = w ? launch_col_w(e, st) : launch_col_fused<V>(e, st);
   }
   if (!rc) rc = launch_epilogue<V>(e, st);
   return rc;
@@ -1276,10 +1361,27 @@ int autotune_impl(pqg_ens* e, cudaStream_t st, double* out) {
     return ms / 3;
   };
   int rc = launch_prologue<V>(e, st);
+  const bool w = warp_on(e);
   // rows
   float best_r = 1e30f;
   int brb = e->rb, btr = e->T_row;
-  for (int rb = 1; rb <= 16 && !rc; rb *= 2) {
+  if (w) {
+    // warp-owned kernels: the warps per CTA, and staged tiles or not
+    int bw = e->w_row;
+    bool bs = e->w_stage;
+    for (int stg = 0; stg < 2; stg++)
+      for (int nw : {2, 4, 8}) {
+        if (rc) break;
+        e->w_row = nw;
+        e->w_stage = stg == 1;
+        if (e->w_stage && !row_staged(e)) continue;
+        const float ms = time3([&]() { launch_row_w(e, false, st); });
+        if (ms < best_r) { best_r = ms; bw = nw; bs = e->w_stage; }
+      }
+    e->w_row = bw;
+    e->w_stage = bs;
+  }
+  for (int rb = 1; rb <= 16 && !rc && !w; rb *= 2) {
     if (e->ny % rb || vsz(e) * ((size_t)e->nx + 3 * (size_t)rb * e->M) > limit) continue;
     for (int tr : {64, 128, 256, 512}) {
       if (tr > 32 * ((rb * e->M + 31) / 32) * 2) continue;
@@ -1294,7 +1396,17 @@ int autotune_impl(pqg_ens* e, cudaStream_t st, double* out) {
   // columns (the fused kernel updates the state: restored below)
   float best_c = 1e30f;
   int bc = e->C, btc = e->T_col;
-  for (int C = 1; C <= 16 && !rc; C *= 2) {
+  if (w) {
+    int bw = e->w_col;
+    for (int nw : {2, 4, 8}) {
+      if (rc) break;
+      e->w_col = nw;
+      const float ms = time3([&]() { launch_col_w(e, st); });
+      if (ms < best_c) { best_c = ms; bw = nw; }
+    }
+    e->w_col = bw;
+  }
+  for (int C = 1; C <= 16 && !rc && !w; C *= 2) {
     if (C > e->nk || vsz(e) * (size_t)e->ny * (1 + 4 * C) > limit) continue;
     for (int tcn : {64, 128, 256, 512}) {
       if (tcn > 2 * e->ny * C) continue;
@@ -1309,7 +1421,7 @@ int autotune_impl(pqg_ens* e, cudaStream_t st, double* out) {
   // whole steps: the per-member kernel (threads 128 .. 512) against the
   // row and column kernels with the shapes just chosen
   float t_two = 0.f, best_m = 0.f;
-  if (!rc && !e->net && member_smem(e)) {
+  if (!rc && !e->net && member_smem(e) && !w) {
     t_two = time3([&]() { step_two<V>(e, 4, st); });
     best_m = 1e30f;
     int bt = e->T_mem, br = e->rb_mem;
@@ -1342,7 +1454,11 @@ int autotune_impl(pqg_ens* e, cudaStream_t st, double* out) {
   e->t = t;
   e->version++;
   drop_graphs_of(e);
-  if (out) {
+  if (out && w) {
+    out[0] = 32 / (e->M / 8) * e->w_row; out[1] = 32 * e->w_row; out[2] = best_r;
+    out[3] = 32 / (e->ny / 8) * e->w_col; out[4] = 32 * e->w_col; out[5] = best_c;
+    out[6] = 0.0; out[7] = 0.0; out[8] = 0.0; out[9] = 0.0;
+  } else if (out) {
     out[0] = e->rb; out[1] = e->T_row; out[2] = best_r;
     out[3] = e->C; out[4] = e->T_col; out[5] = best_c;
     out[6] = member_smem(e) && e->fused && !e->net ? 1.0 : 0.0; out[7] = e->T_mem;

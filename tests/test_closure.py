@@ -215,6 +215,33 @@ def test_ensemble_closure_fp32_runs():
     assert all(np.all(np.isfinite(ens.q(i))) for i in range(8))
 
 
+def test_ensemble_closure_fp32_warp_kernels(monkeypatch):
+    """The FP32 closure ensemble on the warp-owned kernels (the subgrid
+    forcing transformed inside the column kernel) against the block-wide
+    FP32 kernels: the same trajectory up to FP32 rounding, amplified only by
+    the network's BF16 inputs; the closure's own effect is far larger."""
+    import pyqg_gb300 as P
+    from pyqg_gb300.closure import ConvNet, CNNParameterization
+    from pyqg_gb300.coarsen import PHYSICS
+    net = ConvNet(max_batch=4, seed=13)
+    CNNParameterization(net, ([0.0, 0.0], [3e-7, 3e-8], [0.0, 0.0], [3e-13, 3e-14]))
+    rng = np.random.default_rng(14)
+    qs = [1e-7 * rng.standard_normal((2, 64, 64)) for _ in range(4)]
+    out = {}
+    for name, warp, closure in (("warp", "1", True), ("block", "0", True), ("none", "1", False)):
+        monkeypatch.setenv("PQG_ENS_WARP", warp)
+        ens = P.Ensemble([("qg", dict(nx=64, dt=7200.0, **PHYSICS))] * 4, precision="fp32")
+        ens.set_q(qs)
+        if closure:
+            ens.set_closure(net)
+        ens.step(8)
+        out[name] = [ens.q(i) for i in range(4)]
+    for i in range(4):
+        d = rel_l2(out["warp"][i], out["block"][i])
+        assert d < 1e-3, (i, d)
+        assert rel_l2(out["none"][i], out["warp"][i]) > 30 * d
+
+
 @pytest.mark.parametrize("batch", [48, 160])
 def test_forward_many_tiles_per_cta(batch):
     """Batches large enough that every persistent CTA processes several tiles

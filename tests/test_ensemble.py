@@ -174,9 +174,11 @@ def test_large_members_up_to_nx512():
 
 def test_member_kernel_equals_row_and_column_kernels(monkeypatch):
     """The per-member kernel (whole steps of one member per CTA, mixed planes
-    in shared memory) runs the same operations as the row and column
-    kernels: identical states, also through graph replay."""
+    in shared memory) runs the same operations as the block-wide row and
+    column kernels: identical states, also through graph replay.  (FP32
+    groups run the warp-owned kernels unless PQG_ENS_WARP=0.)"""
     import pyqg_gb300 as P
+    monkeypatch.setenv("PQG_ENS_WARP", "0")
     rng = np.random.default_rng(7)
     lay = dict(nz=3, H=[500., 1000., 2500.], U=[0.05, 0.02, 0.0], V=[0., 0., 0.])
     specs = [_qg(1.5e-11, 5.787e-7), _qg(2.0e-11, 3.0e-7), ("layered", dict(nx=64, dt=7200.0, **lay)),
@@ -247,3 +249,55 @@ def test_device_inversion_matrices_match_host_build():
                 scale = np.abs(host).max(axis=(0, 1))
                 scale[0, 0] = 1.0
                 assert (np.abs(dev - host).max(axis=(0, 1)) / scale).max() <= 1e-14, nz
+
+
+def _mixed_specs():
+    lay = dict(nz=3, H=[500., 1000., 2500.], U=[0.05, 0.02, 0.0], V=[0., 0., 0.])
+    return [_qg(1.5e-11, 5.787e-7, nx=16), _qg(1.2e-11, 4.0e-7, nx=32), _qg(1.5e-11, 5.787e-7),
+            ("layered", dict(nx=64, dt=7200.0, **lay)), _qg(1.1e-11, 6.0e-7, nx=128, dt=3600.0),
+            ("layered", dict(nx=128, dt=3600.0, **lay)), _qg(1.5e-11, 5.787e-7, nx=256, dt=3600.0)]
+
+
+def test_warp_kernels_match_block_kernels_and_fp64(monkeypatch):
+    """The warp-owned FP32 row and column kernels (every FP32 group of
+    16 <= nx <= 256 with at most three layers) take the same step as the
+    block-wide FP32 kernels and as the FP64 form, up to FP32 rounding."""
+    import pyqg_gb300 as P
+    rng = np.random.default_rng(31)
+    specs = _mixed_specs()
+    q0 = [1e-7 * rng.standard_normal((3 if k == "layered" else 2, kw["nx"], kw["nx"])) for k, kw in specs]
+    out = {}
+    for name, prec, warp in (("warp", "fp32", "1"), ("block", "fp32", "0"), ("fp64", "fp64", "1")):
+        monkeypatch.setenv("PQG_ENS_WARP", warp)
+        e = P.Ensemble(specs, precision=prec)
+        e.set_q(q0)
+        e.step(3)
+        e.step(37)
+        out[name] = [e.q(i) for i in range(len(specs))]
+    for i in range(len(specs)):
+        ew, eb = rel_l2(out["warp"][i], out["fp64"][i]), rel_l2(out["block"][i], out["fp64"][i])
+        print("member %d: warp %.2e block %.2e against FP64" % (i, ew, eb))
+        assert ew < 1e-5 and eb < 1e-5, i
+        assert rel_l2(out["warp"][i], out["block"][i]) < 1e-5, i
+
+
+def test_warp_kernels_graphs_and_autotune_keep_results(monkeypatch):
+    """FP32 groups on the warp-owned kernels: graph replay, plain launches
+    and an autotuned launch shape give identical states."""
+    a = _two_groups("fp32")
+    b = _two_groups("fp32")
+    a.step(5)
+    b.step(5)
+    choices = b.autotune()
+    assert len(choices) == len(b.groups)
+    for c in choices:
+        assert c["rows_per_cta"] >= 1 and c["cols_per_cta"] >= 1 and c["col_ms"] > 0
+        assert not c["member_kernel"]
+    a.step(40)
+    b.step(40)
+    monkeypatch.setenv("PQG_ENS_NO_GRAPHS", "1")
+    c = _two_groups("fp32")
+    c.step(45)
+    for i in range(3):
+        np.testing.assert_array_equal(a.q(i), b.q(i))
+        np.testing.assert_array_equal(a.q(i), c.q(i))
