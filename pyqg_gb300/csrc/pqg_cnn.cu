@@ -248,8 +248,9 @@ __device__ __forceinline__ void relu_store(const PixOut& o, const float* bias, i
 //                 MMA streams in flight, which the shifted (not atom-aligned)
 //                 operand windows need to reach the tensor pipe's rate.
 // Barriers (parity = use count & 1): hfull / hempty per halo buffer, afull /
-// aempty per accumulator, wfull / wempty per weight stage; the "empty" and
-// "afull" barriers count one arrival per issuer.
+// aempty per accumulator, wfull / wempty per weight stage; hempty, wempty and
+// afull count one arrival per issuer, aempty one per epilogue warp (lane 0,
+// after the warp's TMEM loads and a __syncwarp).
 // ---------------------------------------------------------------------------
 struct HaloArgs {
   int cin;               // input channels
@@ -296,7 +297,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
       tc::mbar_init(&hfull[i], 1);
       tc::mbar_init(&hempty[i], SX);
       tc::mbar_init(&afull[i], SX);
-      tc::mbar_init(&aempty[i], 32 * NEPI);
+      tc::mbar_init(&aempty[i], NEPI);   // one arrival per epilogue warp
     }
     for (int s = 0; s < NST; s++) {
       tc::mbar_init(&wfull[s], 1);
@@ -437,7 +438,8 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
         }
       }
       tc::fence_before();
-      tc::mbar_arrive(&aempty[as]);
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&aempty[as]);
     }
   }
   if (!ok) s_fail = 1;
@@ -573,11 +575,11 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
       tc::mbar_init(&hempty[i], 1);
     }
     for (int i = 0; i < 2; i++)
-      for (int p = 0; p < REPI / 2; p++) tc::mbar_init(&xbar[i][p], 64);
+      for (int p = 0; p < REPI / 2; p++) tc::mbar_init(&xbar[i][p], 2);   // one arrival per warp of the pair
     tc::mbar_init(&drain, 1);
     for (int i = 0; i < NACC; i++) {
       tc::mbar_init(&afull[i], 1);
-      tc::mbar_init(&aempty[i], 32 * REPI);
+      tc::mbar_init(&aempty[i], REPI);   // one arrival per epilogue warp
     }
     for (int s = 0; s < (resident ? nblk : NST); s++) {
       tc::mbar_init(&wfull[s], 1);
@@ -735,7 +737,8 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
           }
         }
         tc::fence_before();
-        tc::mbar_arrive(&aempty[slot]);   // the accumulator is in registers
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&aempty[slot]);   // the accumulator is in registers
         // The horizontal sum rotates the 32 lanes by dx - 2.  The values
         // that the rotation wraps around (tap 0 of lanes 30-31, tap 1 of lane
         // 31, tap 3 of lane 0, tap 4 of lanes 0-1) are used only by pixels of
@@ -754,7 +757,8 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
           xb[2] = make_float4(__uint_as_float(sb[0]), __uint_as_float(sb[1]), __uint_as_float(sb[2]), __uint_as_float(sb[3]));
           xb[3] = make_float4(__uint_as_float(sb[4]), __uint_as_float(sb[5]), __uint_as_float(sb[6]), __uint_as_float(sb[7]));
         }
-        tc::mbar_arrive(&xbar[par][pair]);
+        __syncwarp();   // the warp's edge values are written before its one arrival
+        if (lane == 0) tc::mbar_arrive(&xbar[par][pair]);
         const bool swapped =
             __all_sync(0xffffffffu, tc::mbar_wait(&xbar[par][pair], (aq >> 1) & 1, kLimit, a.ehint));
         if (!swapped) { ok = false; break; }
@@ -1308,7 +1312,7 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
     // about 224 KiB of shared memory.  Two accumulators of SX N columns must
     // fit in TMEM (512).  PQG_CNN_SX caps the width (tuning).
     const size_t budget = 224 * 1024;
-    int cap = 4;
+    int cap = 8;
     if (const char* e = getenv("PQG_CNN_SX")) cap = std::max(1, atoi(e));
     // channel units of at most 64 (PQG_CNN_UNIT=32: of at most 32, for a
     // deeper weight ring beside two halo buffers)
@@ -1318,8 +1322,9 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
     c.cu = cu;
     const size_t wb = (size_t)c.N * cu * 2;
     int best = -1;
-    for (int sx : {4, 2, 1}) {
+    for (int sx : {8, 4, 2, 1}) {
       if (sx > cap || (W % (8 * sx)) || 2 * sx * c.N > 512) continue;
+      if (sx == 8 && kin != 32) continue;   // instantiated for 32 input channels
       for (int nh : {2, 1}) {
         const size_t h = (size_t)nh * halo_bytes(sx, cu);
         if (h >= budget) continue;
@@ -1339,7 +1344,7 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
       int sx = 0, nh = 0, cps = 0;
       const int nread = sscanf(e, "%d,%d,%d", &sx, &nh, &cps);
       if (nread == 3 && cps >= 1 && cps <= 4) c.cps = cps;
-      if (nread >= 2 && (sx == 1 || sx == 2 || sx == 4) && (nh == 1 || nh == 2) &&
+      if (nread >= 2 && (sx == 1 || sx == 2 || sx == 4 || (sx == 8 && kin == 32)) && (nh == 1 || nh == 2) &&
           W % (8 * sx) == 0 && 2 * sx * c.N <= 512) {
         const size_t h = (size_t)nh * halo_bytes(sx, cu);
         if (NTAP * nu <= MAXST && h + (size_t)NTAP * nu * wb <= budget) {
@@ -1393,6 +1398,7 @@ HaloFn halo_kernel(int sx, int ks, int cu) {
     case 8: return cu == 32 ? k_conv_halo<S, 8, 2> : k_conv_halo<S, 8, 4>; \
     default: return nullptr;                                               \
   }
+  if (sx == 8) return ks == 2 ? k_conv_halo<8, 2, 4> : nullptr;   // full 64-pixel rows, 32 input channels
   if (sx == 4) { HK(4) }
   if (sx == 2) { HK(2) }
   if (sx == 1) { HK(1) }
@@ -1523,6 +1529,7 @@ int set_attrs() {
       for (int cu : {64, 32})
         if (cu == 64 || ks >= 4)
           CCUDA(cudaFuncSetAttribute(halo_kernel(sx, ks, cu), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  CCUDA(cudaFuncSetAttribute(halo_kernel(8, 2, 32), cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   for (int kin : {16, 32, 64, 128})
     for (bool small : {false, true})
       CCUDA(cudaFuncSetAttribute(rows_kernel(kin, small), cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 12288));
