@@ -316,17 +316,17 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
   bool ok = true;
   if (warp == NEPI) {
     if (lane == 0) {
-      // producer
-      long long wq = 0;
-      int u = 0;   // pipeline unit: (tile, channel unit)
+      // producer.  Ring positions are kept as (slot, round) counters: the
+      // loop runs on one lane, where a division per tap would dominate.
+      int wq = 0, ws = 0, wr = 0;   // weight blocks issued; ring slot and round
+      int u = 0, hs = 0, hr = 0;    // pipeline unit (tile, channel unit); halo buffer and round
       bool stopped = false;
       for (int tile = blockIdx.x; tile < a.ntiles && ok && !stopped; tile += gridDim.x) {
         const int b = tile / per_img, r = tile - b * per_img;
         const int y0 = (r / a.tiles_x) * TY, x0 = (r % a.tiles_x) * 8 * SX;
         for (int h = 0; h < CH && ok; h++, u++) {
-          const int hs = u % NH;
           if (u == a.stop_unit) { stopped = true; break; }
-          if (u >= NH) ok = tc::mbar_wait(&hempty[hs], ((u - NH) / NH) & 1, a.wait_ns);
+          if (hr > 0) ok = tc::mbar_wait(&hempty[hs], (hr - 1) & 1, a.wait_ns);
           if (!ok) break;
           tc::mbar_expect_tx(&hfull[hs], hbytes);
           for (int gq = 0; gq < groups; gq++)
@@ -340,13 +340,14 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
               }
           } else {
             for (int t = 0; t < NTAP && ok; t++, wq++) {
-              const int ws = (int)(wq % NST);
-              if (wq >= NST) ok = tc::mbar_wait(&wempty[ws], (int)(((wq - NST) / NST) & 1), a.wait_ns);
+              if (wr > 0) ok = tc::mbar_wait(&wempty[ws], (wr - 1) & 1, a.wait_ns);
               if (!ok) break;
               tc::mbar_expect_tx(&wfull[ws], wbytes);
               tc::bulk_load(wst + (size_t)ws * wbytes, a.wpk + (size_t)(t * CH + h) * N * cu, wbytes, &wfull[ws]);
+              if (++ws == NST) { ws = 0; wr++; }
             }
           }
+          if (++hs == NH) { hs = 0; hr++; }
         }
       }
       s_issued[0] = u;
@@ -361,38 +362,42 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
       const uint32_t idesc = tc::idesc_bf16(TM, N);
       const uint64_t ad0 = tc::sdesc(tc::smem_u32(halo), SLAB, TXH * 16) + (uint64_t)(8 * sx);
       const uint64_t bd0 = tc::sdesc(tc::smem_u32(wst), 128, cu * 16);
-      long long wq = 0;
-      int it = 0, u = 0;
+      int ws = 0, wr = 0;   // weight ring slot and round (streamed weights)
+      int hs = 0, hr = 0;   // halo buffer and round
+      int it = 0;
       for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x, it++) {
         const int as = it & 1;
         const uint32_t acc = tmem + as * acc_cols + sx * N;
-        for (int h = 0; h < CH && ok; h++, u++) {
-          const int hs = u % NH;
-          ok = tc::mbar_wait(&hfull[hs], (u / NH) & 1, a.wait_ns);
+        for (int h = 0; h < CH && ok; h++) {
+          ok = tc::mbar_wait(&hfull[hs], hr & 1, a.wait_ns);
           if (ok && h == 0 && it >= 2) ok = tc::mbar_wait(&aempty[as], ((it - 2) >> 1) & 1, a.wait_ns);
           if (!ok) break;
           tc::fence_after();
           const uint64_t adh = ad0 + (uint64_t)hs * (hbytes >> 4);
           int dy = 0, dx = 0;
-          for (int t = 0; t < NTAP && ok; t++, wq++) {
-            const int ws = resident ? t * CH + h : (int)(wq % NST);
+          for (int t = 0; t < NTAP && ok; t++) {
+            const int wsl = resident ? t * CH + h : ws;
             // resident weights: waited for (and fenced) on the first tile only
             if (!resident || it == 0) {
-              ok = tc::mbar_wait(&wfull[ws], resident ? 0 : (int)((wq / NST) & 1), a.wait_ns);
+              ok = tc::mbar_wait(&wfull[wsl], resident ? 0 : wr & 1, a.wait_ns);
               if (!ok) break;
               tc::fence_after();
             }
             const uint64_t at = adh + (uint64_t)(dy * TXH + dx);
-            const uint64_t bt = bd0 + (uint64_t)ws * (wbytes >> 4);
+            const uint64_t bt = bd0 + (uint64_t)wsl * (wbytes >> 4);
 #pragma unroll
             for (int kk = 0; kk < KU; kk++)
               tc::mma_bf16(acc, at + (uint64_t)(kk * (2 * SLAB / 16)), bt + (uint64_t)(16 * kk), idesc,
                            (t | kk | h) ? 1u : 0u);
-            if (!resident) tc::mma_commit(&wempty[ws]);
+            if (!resident) {
+              tc::mma_commit(&wempty[ws]);
+              if (++ws == NST) { ws = 0; wr++; }
+            }
             if (++dx == 5) { dx = 0; dy++; }
           }
           if (!ok) break;
           tc::mma_commit(&hempty[hs]);
+          if (++hs == NH) { hs = 0; hr++; }
         }
         if (!ok) break;
         tc::mma_commit(&afull[as]);
@@ -597,9 +602,9 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
   bool ok = true;
   if (warp == REPI) {
     if (lane == 0) {
-      // producer
-      long long wq = 0;
-      int hq = 0;
+      // producer (ring positions as slot / round counters, as in the halo kernel)
+      int wq = 0, ws = 0, wr = 0;
+      int hq = 0, hs = 0, hr = 0;
       bool first = true;
       for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
         const int b = tile / per_img, y0 = (tile - b * per_img) * RT;
@@ -613,8 +618,7 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
         for (int o = 0; o < NUO && ok; o++) {
           for (int h = 0; h < CH && ok; h++) {
             if (CH > 1 || o == 0) {
-              const int hs = hq % NH;
-              if (hq >= NH) ok = tc::mbar_wait(&hempty[hs], ((hq - NH) / NH) & 1, kLimit, a.hint);
+              if (hr > 0) ok = tc::mbar_wait(&hempty[hs], (hr - 1) & 1, kLimit, a.hint);
               if (!ok) break;
               tc::mbar_expect_tx(&hfull[hs], hbytes);
               // padded rows y0 .. y0 + 5 hold image rows y0 - 2 .. y0 + 3
@@ -622,15 +626,16 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
                 tc::tma_load_4d(halo + (size_t)hs * hbytes + (size_t)gq * RSLAB, &tmap, cu * h + 8 * gq, PAD, y0, b,
                                 &hfull[hs]);
               hq++;
+              if (++hs == NH) { hs = 0; hr++; }
             }
             if (!resident) {
               for (int dy = 0; dy < 5 && ok; dy++, wq++) {
-                const int ws = (int)(wq % NST);
-                if (wq >= NST) ok = tc::mbar_wait(&wempty[ws], (int)(((wq - NST) / NST) & 1), kLimit, a.hint);
+                if (wr > 0) ok = tc::mbar_wait(&wempty[ws], (wr - 1) & 1, kLimit, a.hint);
                 if (!ok) break;
                 tc::mbar_expect_tx(&wfull[ws], wbytes);
                 tc::bulk_load(wst + (size_t)ws * wbytes, a.wpk + (size_t)((o * CH + h) * 5 + dy) * Nu * cu, wbytes,
                               &wfull[ws]);
+                if (++ws == NST) { ws = 0; wr++; }
               }
             }
           }
@@ -647,51 +652,51 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
       const uint32_t idesc = tc::idesc_bf16(TM, Nu);
       const uint64_t ad0 = tc::sdesc(tc::smem_u32(halo), RSLAB, 128);
       const uint64_t bd0 = tc::sdesc(tc::smem_u32(wst), 128, cu * 16);
-      long long wq = 0;
-      int hq = 0, aq = 0, hs = 0;
+      int ws = 0, wr = 0;       // weight ring slot and round
+      int hs = 0, hr = 0;       // halo buffer and round (advanced after each halo unit's last use)
+      int slot = 0, ar = 0;     // accumulator slot and round
       bool first = true;
       for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
-        for (int o = 0; o < NUO && ok; o++, aq++) {
-          const int slot = aq % NACC;
-          if (aq >= NACC) ok = tc::mbar_wait(&aempty[slot], ((aq - NACC) / NACC) & 1, kLimit, a.hint);
+        for (int o = 0; o < NUO && ok; o++) {
+          if (ar > 0) ok = tc::mbar_wait(&aempty[slot], (ar - 1) & 1, kLimit, a.hint);
           if (!ok) break;
           tc::fence_after();
           const uint32_t acc = tmem + slot * Nu;
           for (int h = 0; h < CH && ok; h++) {
             if (CH > 1 || o == 0) {
-              hs = hq % NH;
-              ok = tc::mbar_wait(&hfull[hs], (hq / NH) & 1, kLimit, a.hint);
+              ok = tc::mbar_wait(&hfull[hs], hr & 1, kLimit, a.hint);
               if (!ok) break;
               tc::fence_after();
             }
             const uint64_t adh = ad0 + (uint64_t)hs * (hbytes >> 4);
             for (int dy = 0; dy < 5 && ok; dy++) {
               const int blk = (o * CH + h) * 5 + dy;
-              const int ws = resident ? blk : (int)(wq % NST);
+              const int wsl = resident ? blk : ws;
               if (!resident || first) {
-                ok = tc::mbar_wait(&wfull[ws], resident ? 0 : (int)((wq / NST) & 1), kLimit, a.hint);
+                ok = tc::mbar_wait(&wfull[wsl], resident ? 0 : wr & 1, kLimit, a.hint);
                 if (!ok) break;
                 tc::fence_after();
               }
               const uint64_t at = adh + (uint64_t)(dy * RW);   // dy rows of 64 pixels x 16 bytes
-              const uint64_t bt = bd0 + (uint64_t)ws * (wbytes >> 4);
+              const uint64_t bt = bd0 + (uint64_t)wsl * (wbytes >> 4);
 #pragma unroll
               for (int kk = 0; kk < KU; kk++)
                 tc::mma_bf16(acc, at + (uint64_t)(kk * (2 * RSLAB / 16)), bt + (uint64_t)(16 * kk), idesc,
                              (dy | kk | h) ? 1u : 0u);
               if (!resident) {
                 tc::mma_commit(&wempty[ws]);
-                wq++;
+                if (++ws == NST) { ws = 0; wr++; }
               }
             }
             if (!ok) break;
             if (CH > 1 || o == NUO - 1) {
               tc::mma_commit(&hempty[hs]);
-              hq++;
+              if (++hs == NH) { hs = 0; hr++; }
             }
           }
           if (!ok) break;
           tc::mma_commit(&afull[slot]);
+          if (++slot == NACC) { slot = 0; ar++; }
         }
         first = false;
       }
@@ -704,16 +709,17 @@ __global__ void __launch_bounds__(32 * (REPI + 2)) k_conv_rows(const __grid_cons
     const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
     const int edge = lane < 2 ? lane : (lane >= 30 ? lane - 28 : -1);
     const bool active = SMALL ? grp == 0 : 8 * grp < CO;
-    int aq = 0;
+    int aq = 0, slot = 0, ar = 0;   // accumulators used; slot and round
     for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
       const int b = tile / per_img;
       const int y = (tile - b * per_img) * RT + (quarter >> 1), x = 32 * (quarter & 1) + lane;
       const bool fast = a.e.mode == 0;
       PixOut po{};
       if (fast) po = pix_out(a.e.out_bf, a.e.cout, a.g, b, y, x);
-      for (int o = 0; o < NUO; o++, aq++) {
-        const int slot = aq % NACC, par = aq & 1;
-        const bool got = __all_sync(0xffffffffu, tc::mbar_wait(&afull[slot], (aq / NACC) & 1, kLimit, a.ehint));
+      // (slot, ar) = (aq % NACC, aq / NACC), advanced with aq
+      for (int o = 0; o < NUO; o++, aq++, slot = slot + 1 == NACC ? 0 : slot + 1, ar += slot == 0) {
+        const int par = aq & 1;
+        const bool got = __all_sync(0xffffffffu, tc::mbar_wait(&afull[slot], ar & 1, kLimit, a.ehint));
         if (!got) { ok = false; break; }
         tc::fence_after();
         const uint32_t tacc = trow + slot * Nu;
