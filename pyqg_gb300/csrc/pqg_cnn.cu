@@ -1330,7 +1330,9 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
     int best = -1;
     for (int sx : {8, 4, 2, 1}) {
       if (sx > cap || (W % (8 * sx)) || 2 * sx * c.N > 512) continue;
-      if (sx == 8 && kin != 32) continue;   // instantiated for 32 input channels
+      // eight subtiles: instantiated for 32 input channels; measured faster
+      // than four for N = 16 (the 32 -> 2 output layer) and slower for N = 32
+      if (sx == 8 && (kin != 32 || c.N > 16)) continue;
       for (int nh : {2, 1}) {
         const size_t h = (size_t)nh * halo_bytes(sx, cu);
         if (h >= budget) continue;
