@@ -303,9 +303,9 @@ def test_default_net_learns():
 @pytest.mark.parametrize("channels,batch", [((2, 24, 40, 32, 2), 3), ((2, 128, 64, 32, 32, 2), 40)])
 def test_row_tile_and_halo_kernels_agree(channels, batch, monkeypatch):
     """The row-tile kernel (horizontal taps folded into N) on every layer it
-    takes, the default choice, and the halo kernel (one MMA per tap) on
-    every layer with 64- and with 32-channel input units, on the same
-    network: forward and gradients."""
+    takes and on the 64 -> 32 layer only, and the halo kernel (one MMA per
+    tap, the default) on every layer with 64- and with 32-channel input
+    units, on the same network: forward and gradients."""
     import torch
     from pyqg_gb300.closure import ConvNet
     nets = []
