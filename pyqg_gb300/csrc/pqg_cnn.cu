@@ -69,6 +69,7 @@ constexpr int TY = 16;     // output rows of a halo-kernel tile
 constexpr int TYH = TY + 2 * PAD;
 constexpr int MAXST = 2 * NTAP;   // weight stages of the halo kernel (at most one per tap and unit)
 constexpr int NEPI = 8;           // epilogue warps of the halo kernel (two per TMEM lane quarter)
+constexpr int MAXH = 4;           // halo buffers of the halo kernel at most
 
 thread_local std::string c_last_error;
 
@@ -257,7 +258,7 @@ struct HaloArgs {
   const bf16* wpk;       // 25 per-tap blocks of N x cin (K-major core matrices)
   int N;                 // pad16(cout); 2 SX N <= 512
   int nst;               // weight stages (NTAP: resident)
-  int nh;                // halo buffers (1 or 2)
+  int nh;                // halo buffers (1 .. MAXH)
   int tiles_x;           // W / (8 SX)
   int ntiles;            // batch * (H / 16) * tiles_x
   Img g;
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
   constexpr int KU = KS / CH;              // K steps of 16 per unit
   constexpr int cu = 16 * KU, groups = 2 * KU;   // channels and 8-channel slabs per unit
   extern __shared__ __align__(1024) unsigned char csm[];
-  __shared__ __align__(8) uint64_t hfull[2], hempty[2], afull[2], aempty[2], wfull[MAXST], wempty[MAXST];
+  __shared__ __align__(8) uint64_t hfull[MAXH], hempty[MAXH], afull[2], aempty[2], wfull[MAXST], wempty[MAXST];
   __shared__ __align__(8) uint64_t drain[SX];   // failure path: the MMAs of each issuer
   __shared__ uint32_t tslot;
   __shared__ int s_fail;
@@ -293,9 +294,11 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
   const uint32_t ncols = tmem_cols(2 * acc_cols);
   if (warp == 0) tc::tmem_alloc(&tslot, ncols);
   if (tid == 0) {
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < NH; i++) {
       tc::mbar_init(&hfull[i], 1);
       tc::mbar_init(&hempty[i], SX);
+    }
+    for (int i = 0; i < 2; i++) {
       tc::mbar_init(&afull[i], SX);
       tc::mbar_init(&aempty[i], NEPI);   // one arrival per epilogue warp
     }
@@ -1356,7 +1359,7 @@ void plan_conv(ConvPlan& c, int W, int kin, int nout) {
       int sx = 0, nh = 0, cps = 0;
       const int nread = sscanf(e, "%d,%d,%d", &sx, &nh, &cps);
       if (nread == 3 && cps >= 1 && cps <= 4) c.cps = cps;
-      if (nread >= 2 && (sx == 1 || sx == 2 || sx == 4 || (sx == 8 && kin == 32)) && (nh == 1 || nh == 2) &&
+      if (nread >= 2 && (sx == 1 || sx == 2 || sx == 4 || (sx == 8 && kin == 32)) && nh >= 1 && nh <= MAXH &&
           W % (8 * sx) == 0 && 2 * sx * c.N <= 512) {
         const size_t h = (size_t)nh * halo_bytes(sx, cu);
         if (NTAP * nu <= MAXST && h + (size_t)NTAP * nu * wb <= budget) {
