@@ -148,6 +148,7 @@ def main(only=None):
 
     files.update(physical_parameterizations(pyqg))
     files.update(diagnostics(pyqg))
+    files.update(dataset(pyqg))
     save(files, only)
 
 
@@ -238,6 +239,61 @@ def diagnostics(pyqg):
         rec["names"] = np.array(names)
         out[name] = rec
     return out
+
+
+def _jsonable(v):
+    if v is None:
+        return None
+    a = np.asarray(v)
+    if np.iscomplexobj(a):
+        return {"re": a.real.tolist(), "im": a.imag.tolist()}
+    return a.tolist()
+
+
+def dataset(pyqg):
+    """``Model.to_dataset`` (pyqg/xarray_output.py:118-174) of a short seeded
+    run with every diagnostic filled: the reference module runs unchanged
+    against a stand-in ``xarray`` whose ``Dataset`` records its arguments
+    (xarray is not installed here).  Stored: each data variable's and
+    coordinate's dims, attrs and values, and the global attrs."""
+    import types
+
+    class _Dataset:
+        def __init__(self, data_vars, coords=None, attrs=None):
+            self.data_vars, self.coords, self.attrs = data_vars, coords, dict(attrs or {})
+
+    stub = types.ModuleType("xarray")
+    stub.Dataset = _Dataset
+    saved = sys.modules.get("xarray")
+    sys.modules["xarray"] = stub
+    sys.modules.pop("pyqg.xarray_output", None)
+    try:
+        import pyqg.xarray_output as xo
+        c1 = dict(nx=32, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+                  U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
+        m = pyqg.QGModel(**c1, tavestart=0.0, taveint=7200.0, log_level=0)
+        m.q = 1e-6 * np.random.default_rng(15).standard_normal((2, 32, 32))
+        q0 = np.asarray(m.q).copy()
+        for _ in range(4):
+            m._step_forward()
+        ds = xo.model_to_dataset(m)
+    finally:
+        sys.modules.pop("pyqg.xarray_output", None)
+        if saved is None:
+            sys.modules.pop("xarray", None)
+        else:
+            sys.modules["xarray"] = saved
+    rec = dict(q0=q0, nsteps=np.int64(4))
+    meta = {"vars": {}, "coords": {}}
+    for n, (dims, data, attrs) in ds.data_vars.items():
+        meta["vars"][n] = {"dims": [dims] if isinstance(dims, str) else list(dims), "attrs": attrs}
+        rec["var_" + n] = np.asarray(data)
+    for n, (dims, data, attrs) in ds.coords.items():
+        meta["coords"][n] = {"dims": [dims] if isinstance(dims, str) else list(dims), "attrs": attrs}
+        rec["coord_" + n] = np.asarray(data)
+    meta["attrs"] = {k: _jsonable(v) for k, v in ds.attrs.items()}
+    rec["meta_json"] = np.array(json.dumps(meta))
+    return {"dataset_qg_nx32.npz": rec}
 
 
 if __name__ == "__main__":
