@@ -278,6 +278,64 @@ int pqg_inversion_matrix(int form, int nz, int nl, int nk, const double *S,
 int pqg_advect(pqg_plan *plan, const double *f, const double *u,
                const double *v, int nplanes, double *out_h, void *stream);
 
+/* ---------------------------------------------------------------------
+ * Pointwise stages of the physical parameterizations
+ * (pyqg/parameterizations.py:132-366).  Device arrays: spectral fields
+ * (n, nl, nk) complex (re, im), physical fields (n, ny, nx), wavenumbers
+ * kk (nk) and ll (nl); "3n" = three fields of n planes one after the
+ * other.  The transforms between these stages are pqg_rfft2 /
+ * pqg_irfft2.
+ * Smagorinsky (pyqg/parameterizations.py:165-189):
+ *   pqg_smag_strain:     out3 = [ik uh, il vh, (il uh + ik vh) / 2]
+ *   pqg_smag_stress:     nu = c2dx2 sqrt(2 (Sxx^2 + Syy^2 + 2 Sxy^2)) and
+ *                        p3 = [nu Sxx, nu Sxy, nu Syy] from s3 = [Sxx, Syy,
+ *                        Sxy]; either output may be NULL
+ *   pqg_smag_divergence: out2 = [2 (ik nSxx + il nSxy), 2 (ik nSxy + il nSyy)]
+ * ZannaBolton2020 (pyqg/parameterizations.py:266-285):
+ *   pqg_zb_gradients:    out4 = [ik vh, il vh, ik uh, il uh]
+ *   pqg_zb_products:     from g4 = [vx, vy, ux, uy]: rv = vx - uy,
+ *                        sh = vx + uy, st = ux - vy;
+ *                        out3 = [rv st, rv sh, rv^2 + sh^2 + st^2]
+ *   pqg_zb_combine:      from f3 = fft of those: ss = f3[2] / 2,
+ *                        out2 = kappa [ik (ss - rsh) + il rs,
+ *                                      il (ss + rsh) + ik rs]
+ * BackscatterBiharmonic (pyqg/parameterizations.py:226-236):
+ *   pqg_lap_power:       out = (k^2 + l^2)^power in, power 1 or 2
+ *   pqg_mul_scaled:      out = (a s) b over `count` values
+ *   pqg_backscatter:     out = diss - Cb llp num / (den + eps) with
+ *                        num = sum_z Hi mean(psi diss), den = sum_z Hi
+ *                        mean(psi llp); sums: 2n doubles of device scratch
+ * RingForcing (pyqg/parameterizations.py:338-362):
+ *   pqg_ring_normalize:  out[z] = mag (x - mean x) / mean|x - mean x| for
+ *                        layers with keep[z] != 0, NaN for the others (the
+ *                        reference's 0 / 0); x one plane, moments 2 doubles
+ *                        of device scratch. */
+int pqg_smag_strain(int n, int nl, int nk, const double *kk, const double *ll,
+                    const double *uh, const double *vh, double *out3,
+                    void *stream);
+int pqg_smag_stress(int n, int ny, int nx, const double *s3, double c2dx2,
+                    double *nu, double *p3, void *stream);
+int pqg_smag_divergence(int n, int nl, int nk, const double *kk,
+                        const double *ll, const double *n3, double *out2,
+                        void *stream);
+int pqg_zb_gradients(int n, int nl, int nk, const double *kk, const double *ll,
+                     const double *uh, const double *vh, double *out4,
+                     void *stream);
+int pqg_zb_products(int n, int ny, int nx, const double *g4, double *out3,
+                    void *stream);
+int pqg_zb_combine(int n, int nl, int nk, const double *kk, const double *ll,
+                   const double *f3, double kappa, double *out2, void *stream);
+int pqg_lap_power(int n, int nl, int nk, const double *kk, const double *ll,
+                  int power, const double *in, double *out, void *stream);
+int pqg_mul_scaled(long long count, const double *a, double s, const double *b,
+                   double *out, void *stream);
+int pqg_backscatter(int n, int ny, int nx, const double *psi,
+                    const double *diss, const double *llp, const double *Hi,
+                    double cb, double eps, double *sums, double *out,
+                    void *stream);
+int pqg_ring_normalize(int n, int ny, int nx, const double *x, const int *keep,
+                       double mag, double *moments, double *out, void *stream);
+
 /* Coarse-graining of one state (no counterpart in the reference): the fine
  * spectral PV qh_f (nz, ny_f, nx_f/2+1) is truncated sharply to the coarse
  * plan's grid (|k| < nx_c/2, |l| < ny_c/2, amplitudes kept) giving q_c

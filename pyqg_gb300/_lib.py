@@ -94,6 +94,16 @@ SIGNATURES = {
     "pqg_inversion_matrix": (_I, [_I, _I, _I, _I, _P, _P, _P, _P, _P]),
     "pqg_diag_accumulate": (_I, [_P, _I, ctypes.POINTER(DiagFields), _P, _P]),
     "pqg_coarse_forcing": (_I, [_P, _P, _P, _P, _P, _P]),
+    "pqg_smag_strain": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "pqg_smag_stress": (_I, [_I, _I, _I, _P, _D, _P, _P, _P]),
+    "pqg_smag_divergence": (_I, [_I, _I, _I, _P, _P, _P, _P, _P]),
+    "pqg_zb_gradients": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "pqg_zb_products": (_I, [_I, _I, _I, _P, _P, _P]),
+    "pqg_zb_combine": (_I, [_I, _I, _I, _P, _P, _P, _D, _P, _P]),
+    "pqg_lap_power": (_I, [_I, _I, _I, _P, _P, _I, _P, _P, _P]),
+    "pqg_mul_scaled": (_I, [ctypes.c_longlong, _P, _D, _P, _P, _P]),
+    "pqg_backscatter": (_I, [_I, _I, _I, _P, _P, _P, _P, _D, _D, _P, _P, _P]),
+    "pqg_ring_normalize": (_I, [_I, _I, _I, _P, _P, _D, _P, _P, _P]),
     "pqg_cnn_last_error": (ctypes.c_char_p, []),
     "pqg_cnn_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _I, _I]),
     "pqg_cnn_destroy": (_I, [_P]),

@@ -1378,6 +1378,9 @@ PQG_API int pqg_version(void) { return 100; }
 
 PQG_API const char* pqg_last_error(void) { return g_last_error.c_str(); }
 
+// error status for the library's other translation units (not part of the C API)
+int pqg_report_error(int code, const char* msg) { return fail(code, msg); }
+
 PQG_API int pqg_plan_create(pqg_plan** out, int nz, int ny, int nx) {
   if (!out) return fail(PQG_ERR_INVALID, "plan output pointer is NULL");
   *out = nullptr;

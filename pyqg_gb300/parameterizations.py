@@ -6,13 +6,19 @@ A parameterization is a callable taking the model and returning either a
 
 The physical closures below run on the GPU: their inputs are the model's
 device fields, their transforms the model's CUDA transforms and their
-pointwise arithmetic CUDA tensors.  Called by the model's step (the hook)
-they return CUDA tensors, which the step consumes without a host copy;
-called directly they return numpy arrays, as the reference's do.
+pointwise stages the library's kernels (``pqg_smag_*``, ``pqg_zb_*``,
+``pqg_lap_power``, ``pqg_mul_scaled``, ``pqg_backscatter``,
+``pqg_ring_normalize``); PyTorch only allocates their device buffers.
+Called by the model's step (the hook) they return CUDA tensors, which the
+step consumes without a host copy; called directly they return numpy
+arrays, as the reference's do.
 """
+import ctypes
 from abc import ABC, abstractmethod
 
 import numpy as np
+
+from . import _lib
 
 __all__ = ["Parameterization", "CompositeParameterization",
            "WeightedParameterization", "UVParameterization",
@@ -30,6 +36,20 @@ def _dev(m, name):
         t = torch.from_numpy(np.ascontiguousarray(val)).to(m._device)
         cache[name] = t
     return t
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _empty(m, shape, complex_=False):
+    import torch
+    return torch.empty(shape, dtype=torch.complex128 if complex_ else torch.float64, device=m._device)
+
+
+def _run(m, name, *args):
+    """Call library entry point `name` on the model's stream."""
+    _lib.check(getattr(_lib.lib(), name)(*args, m._sp()))
 
 
 def _as_output(m, x):
@@ -128,33 +148,43 @@ class QParameterization(Parameterization):
 class Smagorinsky(UVParameterization):
     r"""Smagorinsky (1963) eddy viscosity
     nu = (C_S dx)^2 sqrt(2 (Sxx^2 + Syy^2 + 2 Sxy^2)), forcing
-    du = 2 (d_x(nu Sxx) + d_y(nu Sxy)), dv = 2 (d_x(nu Sxy) + d_y(nu Syy))."""
+    du = 2 (d_x(nu Sxx) + d_y(nu Sxy)), dv = 2 (d_x(nu Sxy) + d_y(nu Syy))
+    (pyqg/parameterizations.py:132-192)."""
 
     def __init__(self, constant=0.1):
         self.constant = constant
 
-    def _viscosity(self, m):
+    def _viscosity(self, m, stresses):
+        """Device nu (nz, ny, nx) and, if `stresses`, the three stress
+        fields nu Sxx, nu Sxy, nu Syy as one (3 nz, ny, nx) array."""
         import torch
-        ik, il = _dev(m, "ik"), _dev(m, "il")
-        uh = m.fft(m.device_field("u"))
-        vh = m.fft(m.device_field("v"))
-        Sxx = m.ifft(uh * ik)
-        Syy = m.ifft(vh * il)
-        Sxy = 0.5 * m.ifft(uh * il + vh * ik)
-        nu = (self.constant * m.dx) ** 2 * torch.sqrt(2 * (Sxx ** 2 + Syy ** 2 + 2 * Sxy ** 2))
-        return nu, Sxx, Syy, Sxy
+        with torch.cuda.stream(m._stream):
+            uh = m.fft(m.device_field("u"))
+            vh = m.fft(m.device_field("v"))
+            n, nl, nk = uh.shape
+            kk, ll = _dev(m, "kk"), _dev(m, "ll")
+            strain_h = _empty(m, (3 * n, nl, nk), True)
+            _run(m, "pqg_smag_strain", n, nl, nk, _p(kk), _p(ll), _p(uh), _p(vh), _p(strain_h))
+            strain = m._device_irfft2(strain_h)
+            nu = _empty(m, (n, m.ny, m.nx))
+            p3 = _empty(m, (3 * n, m.ny, m.nx)) if stresses else None
+            _run(m, "pqg_smag_stress", n, m.ny, m.nx, _p(strain), float((self.constant * m.dx) ** 2), _p(nu),
+                 _p(p3) if stresses else None)
+        return nu, p3
 
     def __call__(self, m, just_viscosity=False):
-        nu, Sxx, Syy, Sxy = self._viscosity(m)
+        import torch
+        nu, p3 = self._viscosity(m, not just_viscosity)
         if just_viscosity:
             return _as_output(m, nu)
-        ik, il = _dev(m, "ik"), _dev(m, "il")
-        nSxx = m.fft(nu * Sxx)
-        nSxy = m.fft(nu * Sxy)
-        nSyy = m.fft(nu * Syy)
-        du = 2 * (m.ifft(nSxx * ik) + m.ifft(nSxy * il))
-        dv = 2 * (m.ifft(nSxy * ik) + m.ifft(nSyy * il))
-        return _as_output(m, (du, dv))
+        with torch.cuda.stream(m._stream):
+            n = nu.shape[0]
+            n3 = m._device_rfft2(p3)
+            kk, ll = _dev(m, "kk"), _dev(m, "ll")
+            d2 = _empty(m, (2 * n, m.nl, m.nk), True)
+            _run(m, "pqg_smag_divergence", n, m.nl, m.nk, _p(kk), _p(ll), _p(n3), _p(d2))
+            duv = m._device_irfft2(d2)
+        return _as_output(m, (duv[:n], duv[n:]))
 
     def __repr__(self):
         return f"Smagorinsky(Cs={self.constant})"
@@ -171,18 +201,27 @@ class BackscatterBiharmonic(QParameterization):
         self.eps = eps
 
     def __call__(self, m):
-        ik, il = _dev(m, "ik"), _dev(m, "il")
-        Hi = _dev(m, "Hi")
-        ph = m.device_field("ph")
-        lap = ik ** 2 + il ** 2
-        psi = m.ifft(ph)
-        lap_lap_psi = m.ifft(lap ** 2 * ph)
-        nu = self.smagorinsky._viscosity(m)[0]
-        dissipation = -m.ifft(lap * m.fft(lap_lap_psi * m.dx ** 2 * nu))
-        num = (Hi * (psi * dissipation).mean(dim=(-1, -2))).sum()
-        den = (Hi * (psi * lap_lap_psi).mean(dim=(-1, -2))).sum() + self.eps
-        backscatter = -self.back_constant * lap_lap_psi * (num / den)
-        return _as_output(m, dissipation + backscatter)
+        import torch
+        with torch.cuda.stream(m._stream):
+            ph = m.device_field("ph")
+            n, nl, nk = ph.shape
+            kk, ll = _dev(m, "kk"), _dev(m, "ll")
+            psi = m._device_irfft2(ph)
+            lap2_ph = _empty(m, (n, nl, nk), True)
+            _run(m, "pqg_lap_power", n, nl, nk, _p(kk), _p(ll), 2, _p(ph), _p(lap2_ph))
+            lap_lap_psi = m._device_irfft2(lap2_ph)
+            nu = self.smagorinsky._viscosity(m, False)[0]
+            x = _empty(m, (n, m.ny, m.nx))
+            _run(m, "pqg_mul_scaled", n * m.ny * m.nx, _p(lap_lap_psi), float(m.dx ** 2), _p(nu), _p(x))
+            xh = m._device_rfft2(x)
+            yh = _empty(m, (n, nl, nk), True)
+            _run(m, "pqg_lap_power", n, nl, nk, _p(kk), _p(ll), 1, _p(xh), _p(yh))
+            dissipation = m._device_irfft2(yh)      # -ifft(lap X) with lap = -(k^2 + l^2)
+            sums = _empty(m, (2 * n,))
+            out = _empty(m, (n, m.ny, m.nx))
+            _run(m, "pqg_backscatter", n, m.ny, m.nx, _p(psi), _p(dissipation), _p(lap_lap_psi),
+                 _p(_dev(m, "Hi")), float(self.back_constant), float(self.eps), _p(sums), _p(out))
+        return _as_output(m, out)
 
     def __repr__(self):
         return (f"BackscatterBiharmonic(Cs={self.smagorinsky.constant}, "
@@ -196,23 +235,22 @@ class ZannaBolton2020(UVParameterization):
         self.constant = constant
 
     def __call__(self, m):
-        ik, il = _dev(m, "ik"), _dev(m, "il")
-        uh = m.fft(m.device_field("u"))
-        vh = m.fft(m.device_field("v"))
-        vx = m.ifft(vh * ik)
-        vy = m.ifft(vh * il)
-        ux = m.ifft(uh * ik)
-        uy = m.ifft(uh * il)
-        rel_vort = vx - uy
-        shearing = vx + uy
-        stretching = ux - vy
-        rv_stretch = m.fft(rel_vort * stretching)
-        rv_shear = m.fft(rel_vort * shearing)
-        sum_sqs = m.fft(rel_vort ** 2 + shearing ** 2 + stretching ** 2) / 2.0
-        kappa = self.constant
-        du = kappa * m.ifft(ik * (sum_sqs - rv_shear) + il * rv_stretch)
-        dv = kappa * m.ifft(il * (sum_sqs + rv_shear) + ik * rv_stretch)
-        return _as_output(m, (du, dv))
+        import torch
+        with torch.cuda.stream(m._stream):
+            uh = m.fft(m.device_field("u"))
+            vh = m.fft(m.device_field("v"))
+            n, nl, nk = uh.shape
+            kk, ll = _dev(m, "kk"), _dev(m, "ll")
+            grad_h = _empty(m, (4 * n, nl, nk), True)
+            _run(m, "pqg_zb_gradients", n, nl, nk, _p(kk), _p(ll), _p(uh), _p(vh), _p(grad_h))
+            grad = m._device_irfft2(grad_h)        # vx, vy, ux, uy
+            prod = _empty(m, (3 * n, m.ny, m.nx))
+            _run(m, "pqg_zb_products", n, m.ny, m.nx, _p(grad), _p(prod))
+            prod_h = m._device_rfft2(prod)
+            d2 = _empty(m, (2 * n, nl, nk), True)
+            _run(m, "pqg_zb_combine", n, nl, nk, _p(kk), _p(ll), _p(prod_h), float(self.constant), _p(d2))
+            duv = m._device_irfft2(d2)
+        return _as_output(m, (duv[:n], duv[n:]))
 
     def __repr__(self):
         return f"ZannaBolton2020(κ={self.constant:.2e})"
@@ -238,18 +276,21 @@ class RingForcing(QParameterization):
         mask[wvx > self.k_out_forc] = 0.
         # the random draws stay on numpy's generator, as in the reference
         ring_hat = mask * (np.random.randn(nhx, nhy) + 1j * np.random.randn(nhx, nhy))
-        one = m.ifft(torch.from_numpy(ring_hat[np.newaxis]).to(m._device))
-        ring = one.expand(m.nz, m.ny, m.nx).clone()
+        keep = np.ones(m.nz, dtype=np.int32)
         if self.layers != 'all':
-            keep = torch.zeros((m.nz, 1, 1), dtype=ring.dtype, device=ring.device)
+            keep[:] = 0
             if self.layers == 'surf':
-                keep[0] = 1.0
+                keep[0] = 1
             elif self.layers == 'bottom':
-                keep[-1] = 1.0
-            ring = ring * keep
-        ring = ring - ring.mean(dim=(-1, -2), keepdim=True)
-        ring = ring / ring.abs().mean(dim=(-1, -2), keepdim=True)
-        return _as_output(m, self.mag_noise_forc * ring)
+                keep[-1] = 1
+        with torch.cuda.stream(m._stream):
+            one = m.ifft(torch.from_numpy(ring_hat[np.newaxis]).to(m._device))
+            keep_d = torch.from_numpy(keep).to(m._device)
+            moments = _empty(m, (2,))
+            out = _empty(m, (m.nz, m.ny, m.nx))
+            _run(m, "pqg_ring_normalize", m.nz, m.ny, m.nx, _p(one), _p(keep_d), float(self.mag_noise_forc),
+                 _p(moments), _p(out))
+        return _as_output(m, out)
 
     def __repr__(self):
         return f"RingForcing(k_in_forc={self.k_in_forc}, k_out_forc={self.k_out_forc})"
