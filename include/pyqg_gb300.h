@@ -300,7 +300,7 @@ int pqg_advect(pqg_plan *plan, const double *f, const double *u,
  *                        out2 = kappa [ik (ss - rsh) + il rs,
  *                                      il (ss + rsh) + ik rs]
  * BackscatterBiharmonic (pyqg/parameterizations.py:226-236):
- *   pqg_lap_power:       out = (k^2 + l^2)^power in, power 1 or 2
+ *   pqg_lap_power:       out = scale (k^2 + l^2)^power in, power 1 or 2
  *   pqg_mul_scaled:      out = (a s) b over `count` values
  *   pqg_backscatter:     out = diss - Cb llp num / (den + eps) with
  *                        num = sum_z Hi mean(psi diss), den = sum_z Hi
@@ -326,7 +326,15 @@ int pqg_zb_products(int n, int ny, int nx, const double *g4, double *out3,
 int pqg_zb_combine(int n, int nl, int nk, const double *kk, const double *ll,
                    const double *f3, double kappa, double *out2, void *stream);
 int pqg_lap_power(int n, int nl, int nk, const double *kk, const double *ll,
-                  int power, const double *in, double *out, void *stream);
+                  int power, double scale, const double *in, double *out,
+                  void *stream);
+/* out[i] = sum_j m[i][j] in[j] (j in order) for planes of `plane` doubles
+ * (a complex plane counts re and im); m is a host nout x nin row-major
+ * matrix, at most 8 x 8.  The layer combinations of the device
+ * diagnostics: S ph, the modal projection, p1 - p2 and del1 u1 + del2 u2
+ * (pyqg/qg_model.py:231-263, pyqg/layered_model.py:261-300). */
+int pqg_layer_mix(int nout, int nin, long long plane, const double *m,
+                  const double *in, double *out, void *stream);
 int pqg_mul_scaled(long long count, const double *a, double s, const double *b,
                    double *out, void *stream);
 int pqg_backscatter(int n, int ny, int nx, const double *psi,

@@ -100,7 +100,8 @@ SIGNATURES = {
     "pqg_zb_gradients": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _P]),
     "pqg_zb_products": (_I, [_I, _I, _I, _P, _P, _P]),
     "pqg_zb_combine": (_I, [_I, _I, _I, _P, _P, _P, _D, _P, _P]),
-    "pqg_lap_power": (_I, [_I, _I, _I, _P, _P, _I, _P, _P, _P]),
+    "pqg_lap_power": (_I, [_I, _I, _I, _P, _P, _I, _D, _P, _P, _P]),
+    "pqg_layer_mix": (_I, [_I, _I, ctypes.c_longlong, _P, _P, _P, _P]),
     "pqg_mul_scaled": (_I, [ctypes.c_longlong, _P, _D, _P, _P, _P]),
     "pqg_backscatter": (_I, [_I, _I, _I, _P, _P, _P, _P, _D, _D, _P, _P, _P]),
     "pqg_ring_normalize": (_I, [_I, _I, _I, _P, _P, _D, _P, _P, _P]),

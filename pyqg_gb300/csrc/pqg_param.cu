@@ -127,14 +127,33 @@ __global__ void k_zb_comb(long long S, int nl, int nk, const double* kk, const d
   }
 }
 
-// out = (k^2 + l^2)^power in (power 1 or 2): the biharmonic operator lap^2
-// and -lap of the backscatter closure, with lap = (ik)^2 + (il)^2
-__global__ void k_lap(long long S, int nl, int nk, const double* kk, const double* ll, int power, const double* in,
-                      double* out) {
+// out = scale (k^2 + l^2)^power in (power 1 or 2): the biharmonic operator
+// lap^2 and -lap of the backscatter closure, with lap = (ik)^2 + (il)^2,
+// and -wv2 ph of the diagnostics
+__global__ void k_lap(long long S, int nl, int nk, const double* kk, const double* ll, int power, double scale,
+                      const double* in, double* out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < S; i += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(i % nk), l = (int)((i / nk) % nl);
     const double w = __dadd_rn(__dmul_rn(kk[k], kk[k]), __dmul_rn(ll[l], ll[l]));
-    st2(out, i, cscal(power == 2 ? __dmul_rn(w, w) : w, ld2(in, i)));
+    st2(out, i, cscal(scale, cscal(power == 2 ? __dmul_rn(w, w) : w, ld2(in, i))));
+  }
+}
+
+// out[i] = sum_j m[i][j] in[j] over planes of `plane` doubles (a complex
+// plane counts its re and im), j in order
+constexpr int kMixMax = 8;
+struct Mix {
+  double m[kMixMax * kMixMax];
+};
+__global__ void k_layer_mix(int nout, int nin, long long plane, Mix mx, const double* in, double* out) {
+  const long long total = (long long)nout * plane;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / plane);
+    const long long p = t - (long long)i * plane;
+    double acc = 0.0;
+    for (int j = 0; j < nin; j++) acc = __dadd_rn(acc, __dmul_rn(mx.m[i * kMixMax + j], in[j * plane + p]));
+    out[t] = acc;
   }
 }
 
@@ -288,13 +307,25 @@ PQG_API int pqg_zb_combine(int n, int nl, int nk, const double* kk, const double
   return launch_check("pqg_zb_combine");
 }
 
-PQG_API int pqg_lap_power(int n, int nl, int nk, const double* kk, const double* ll, int power, const double* in,
-                          double* out, void* stream) {
+PQG_API int pqg_lap_power(int n, int nl, int nk, const double* kk, const double* ll, int power, double scale,
+                          const double* in, double* out, void* stream) {
   if (n < 1 || nl < 1 || nk < 1 || !kk || !ll || !in || !out || (power != 1 && power != 2))
     return pqg_report_error(PQG_ERR_INVALID, "pqg_lap_power: bad argument");
   const long long S = (long long)n * nl * nk;
-  k_lap<<<blocks_for(S), kThreads, 0, (cudaStream_t)stream>>>(S, nl, nk, kk, ll, power, in, out);
+  k_lap<<<blocks_for(S), kThreads, 0, (cudaStream_t)stream>>>(S, nl, nk, kk, ll, power, scale, in, out);
   return launch_check("pqg_lap_power");
+}
+
+PQG_API int pqg_layer_mix(int nout, int nin, long long plane, const double* m, const double* in, double* out,
+                          void* stream) {
+  if (nout < 1 || nin < 1 || nout > kMixMax || nin > kMixMax || plane < 1 || !m || !in || !out)
+    return pqg_report_error(PQG_ERR_INVALID, "pqg_layer_mix: bad argument (at most 8 x 8 layers)");
+  Mix mx = {};
+  for (int i = 0; i < nout; i++)
+    for (int j = 0; j < nin; j++) mx.m[i * kMixMax + j] = m[i * nin + j];
+  k_layer_mix<<<blocks_for((long long)nout * plane), kThreads, 0, (cudaStream_t)stream>>>(nout, nin, plane, mx, in,
+                                                                                        out);
+  return launch_check("pqg_layer_mix");
 }
 
 PQG_API int pqg_mul_scaled(long long count, const double* a, double s, const double* b, double* out, void* stream) {

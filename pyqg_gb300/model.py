@@ -527,8 +527,27 @@ class Model(PseudoSpectralKernel):
 
     def _device_derived(self, needs):
         """Derived fields of the diagnostics, on the device (the device
-        counterpart of ``_calc_derived_fields``)."""
+        counterpart of ``_calc_derived_fields``); layer combinations and
+        spectral scalings by ``pqg_layer_mix`` and ``pqg_lap_power``."""
+        import ctypes
         import torch
+        from . import _lib
+        from .parameterizations import _dev
+        L = _lib.lib()
+
+        def ptr(t):
+            return ctypes.c_void_p(t.data_ptr())
+
+        def mix(mat, x):
+            """sum_j mat[i][j] x[j] for (n, ...) device x."""
+            mat = np.ascontiguousarray(np.atleast_2d(np.asarray(mat, dtype=np.float64)))
+            x = x.contiguous()
+            plane = x[0].numel() * (2 if x.is_complex() else 1)
+            out = torch.empty((mat.shape[0],) + tuple(x.shape[1:]), dtype=x.dtype, device=self._device)
+            _lib.check(L.pqg_layer_mix(mat.shape[0], mat.shape[1], plane, mat.ctypes.data, ptr(x), ptr(out),
+                                       self._sp()))
+            return out
+
         f = {}
         ph = self.device_field("ph")
         u, v = self.device_field("u"), self.device_field("v")
@@ -536,22 +555,21 @@ class Model(PseudoSpectralKernel):
             if 'Jq' in needs:
                 f['Jq'] = self._device_advect(self.device_field("q"), u, v)
             if 'Jpxi' in needs:
-                wv2 = torch.from_numpy(np.ascontiguousarray(self.wv2)).to(self._device)
-                xi = self._device_irfft2(-wv2 * ph)
-                f['Jpxi'] = self._device_advect(xi, u, v)
+                # xi = ifft(-wv2 ph)
+                neg_wv2_ph = torch.empty_like(ph)
+                _lib.check(L.pqg_lap_power(ph.shape[0], self.nl, self.nk, ptr(_dev(self, "kk")),
+                                           ptr(_dev(self, "ll")), 1, -1.0, ptr(ph), ptr(neg_wv2_ph), self._sp()))
+                f['Jpxi'] = self._device_advect(self._device_irfft2(neg_wv2_ph), u, v)
             if 'Jptpc' in needs:
                 p = self._device_irfft2(ph)
-                f['Jptpc'] = -self._device_advect(
-                    (p[0] - p[1])[None], (self.del1 * u[0] + self.del2 * u[1])[None],
-                    (self.del1 * v[0] + self.del2 * v[1])[None])[0]
+                w = [[self.del1, self.del2]]
+                f['Jptpc'] = mix([[-1.0]], self._device_advect(mix([[1.0, -1.0]], p), mix(w, u), mix(w, v)))[0]
             if 'Sph' in needs or 'JSp' in needs:
-                S = torch.from_numpy(np.ascontiguousarray(self.S, dtype=np.float64)).to(self._device)
-                f['Sph'] = torch.einsum("ij,jkl->ikl", S.to(ph.dtype), ph).contiguous()
+                f['Sph'] = mix(self.S, ph)
                 if 'JSp' in needs:
                     f['JSp'] = self._device_advect(self._device_irfft2(f['Sph']), u, v)
             if 'phn' in needs:
-                pinv = torch.from_numpy(np.ascontiguousarray(np.linalg.inv(self.pmodes))).to(self._device)
-                f['phn'] = torch.einsum("ij,jkl->ikl", pinv.to(ph.dtype), ph).contiguous()
+                f['phn'] = mix(np.linalg.inv(self.pmodes), ph)
         return f
 
     def _accumulate_device_diagnostics(self, items):

@@ -208,14 +208,14 @@ class BackscatterBiharmonic(QParameterization):
             kk, ll = _dev(m, "kk"), _dev(m, "ll")
             psi = m._device_irfft2(ph)
             lap2_ph = _empty(m, (n, nl, nk), True)
-            _run(m, "pqg_lap_power", n, nl, nk, _p(kk), _p(ll), 2, _p(ph), _p(lap2_ph))
+            _run(m, "pqg_lap_power", n, nl, nk, _p(kk), _p(ll), 2, 1.0, _p(ph), _p(lap2_ph))
             lap_lap_psi = m._device_irfft2(lap2_ph)
             nu = self.smagorinsky._viscosity(m, False)[0]
             x = _empty(m, (n, m.ny, m.nx))
             _run(m, "pqg_mul_scaled", n * m.ny * m.nx, _p(lap_lap_psi), float(m.dx ** 2), _p(nu), _p(x))
             xh = m._device_rfft2(x)
             yh = _empty(m, (n, nl, nk), True)
-            _run(m, "pqg_lap_power", n, nl, nk, _p(kk), _p(ll), 1, _p(xh), _p(yh))
+            _run(m, "pqg_lap_power", n, nl, nk, _p(kk), _p(ll), 1, 1.0, _p(xh), _p(yh))
             dissipation = m._device_irfft2(yh)      # -ifft(lap X) with lap = -(k^2 + l^2)
             sums = _empty(m, (2 * n,))
             out = _empty(m, (n, m.ny, m.nx))
