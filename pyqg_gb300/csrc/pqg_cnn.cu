@@ -377,6 +377,29 @@ __global__ void __launch_bounds__(32 * (NEPI + 1 + SX)) k_conv_halo(const __grid
           if (!ok) break;
           tc::fence_after();
           const uint64_t adh = ad0 + (uint64_t)hs * (hbytes >> 4);
+          if (KU >= 2 && resident && it > 0) {
+            // steady state with resident weights and two or more MMAs per
+            // tap: no waits or branches inside the tile (32 -> 32: 134
+            // against 148 us; the one-MMA-per-tap first layer is slower this
+            // way and keeps the general loop).  The loop stays rolled: fully
+            // unrolled, the same body gave wrong results on a CTA's later
+            // tiles, deterministically (the same error with a sleep after
+            // every tap), so a code-generation effect rather than a race.
+            const uint64_t bdh = bd0 + (uint64_t)h * (wbytes >> 4);
+            const uint64_t wstep = (uint64_t)CH * (wbytes >> 4);
+#pragma unroll 1
+            for (int t = 0; t < NTAP; t++) {
+              const uint64_t at = adh + (uint64_t)((t / 5) * TXH + t % 5);
+              const uint64_t bt = bdh + (uint64_t)t * wstep;
+#pragma unroll
+              for (int kk = 0; kk < KU; kk++)
+                tc::mma_bf16(acc, at + (uint64_t)(kk * (2 * SLAB / 16)), bt + (uint64_t)(16 * kk), idesc,
+                             (t | kk | h) ? 1u : 0u);
+            }
+            tc::mma_commit(&hempty[hs]);
+            if (++hs == NH) { hs = 0; hr++; }
+            continue;
+          }
           int dy = 0, dx = 0;
           for (int t = 0; t < NTAP && ok; t++) {
             const int wsl = resident ? t * CH + h : ws;
