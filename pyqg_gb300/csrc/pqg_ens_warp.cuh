@@ -15,8 +15,9 @@
 // planes, the products, R2C of uq, vq); the column kernel gives every group
 // one spectral column of one member with all of its layers, so the layer
 // inversion and the Adams-Bashforth update run in registers without
-// clusters.  Every warp works on its own rows or columns: the only block
-// barrier orders the twiddle table's copy into shared memory.
+// clusters.  Every warp transforms its own rows or columns; block barriers
+// only order the twiddle table's copy into shared memory and, in the staged
+// row kernel, the CTA's coalesced tile loads and stores around them.
 
 namespace wg {
 
@@ -150,6 +151,8 @@ __device__ __forceinline__ void r2c_out(const float2 (&Z)[8], float2* X, int sx,
 // threads on consecutive rows (RB x 8 contiguous bytes per k), and the
 // groups read and write their own row of the tile.  STAGE needs RB | ny.
 // ---------------------------------------------------------------------------
+// Register caps: 85 for the staged kernel (no spills), 128 otherwise;
+// measured faster than the compiler's unbounded choice (up to 125).
 template <int LOGM, bool STAGE>
 __global__ void __launch_bounds__(256, STAGE ? 3 : 2) e_row_w(EGeo g, EConsts<float> c, float2* scratch, const float* qphys,
                                                   const float2* __restrict__ twx, float scale, float* qout) {
@@ -254,6 +257,8 @@ __global__ void __launch_bounds__(256, STAGE ? 3 : 2) e_row_w(EGeo g, EConsts<fl
 // the current qh of every layer have all been formed before the first
 // update.
 // ---------------------------------------------------------------------------
+// Register cap 128 (three layers spill 40-260 bytes): measured faster than
+// the unbounded 170-255 registers, which leave 8-16 warps per SM.
 template <int LOGN, int NZ>
 __global__ void __launch_bounds__(256, 2) e_col_w(EGeo g, EConsts<float> c, float2* scratch, float2* qh,
                                                const float2* dqp, float2* dqpp, const float2* __restrict__ twy,
