@@ -591,6 +591,11 @@ class Model(PseudoSpectralKernel):
         def harr(x, n):
             if x is None:
                 return None
+            x = np.asarray(x)
+            if np.iscomplexobj(x):
+                # eigenvalue-derived constants (kdi2 of the layered model)
+                # are real numbers held in a complex array
+                x = x.real
             a = np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64).ravel(), (n,)))
             keep.append(a)
             return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
