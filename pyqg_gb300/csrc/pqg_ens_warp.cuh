@@ -151,10 +151,11 @@ __device__ __forceinline__ void r2c_out(const float2 (&Z)[8], float2* X, int sx,
 // threads on consecutive rows (RB x 8 contiguous bytes per k), and the
 // groups read and write their own row of the tile.  STAGE needs RB | ny.
 // ---------------------------------------------------------------------------
-// Register caps: 85 for the staged kernel (no spills), 128 otherwise;
-// measured faster than the compiler's unbounded choice (up to 125).
+// Register caps: 64 for the staged kernel (spills of 20-52 bytes at
+// M = 64, 128; config 3 0.66 against 0.68 ms with 85), 128 otherwise;
+// both measured faster than the compiler's unbounded choice (up to 125).
 template <int LOGM, bool STAGE>
-__global__ void __launch_bounds__(256, STAGE ? 3 : 2) e_row_w(EGeo g, EConsts<float> c, float2* scratch, const float* qphys,
+__global__ void __launch_bounds__(256, STAGE ? 4 : 2) e_row_w(EGeo g, EConsts<float> c, float2* scratch, const float* qphys,
                                                   const float2* __restrict__ twx, float scale, float* qout) {
   constexpr int M = 1 << LOGM, G = M / 8, RPW = 32 / G, N = 2 * M, SG = wg::wstride(M);
   extern __shared__ __align__(16) unsigned char esm[];
