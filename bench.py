@@ -1,5 +1,5 @@
 """Benchmark of the FP64 pseudo-spectral step (two-layer QG, nx=ny=256,
-dt=3600 s: the config-2 physics) in simulated years per wall-clock hour.
+dt=3600 s) in simulated years per wall-clock hour.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -27,7 +27,7 @@ sys.path.insert(0, HERE)
 
 YEAR = 360 * 86400.0          # pyqg/tests/test_reference_solns.py:12
 METRIC = "sim-yr/hr, 1 GB300: nx64+learned closure vs nx256 plain at matched KE error"
-C2 = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
+TWO_LAYER = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
           U2=0.0, rek=5.787e-7, filterfac=23.6)
 QUIET = dict(tavestart=1e30, taveint=1e30, log_level=0)
 
@@ -167,7 +167,7 @@ def _ref_kernel(mod, fft_workers):
 
 
 def cpu_model_steps(nsteps, nx=256, dt=3600.0, seed=0, threads=None, fft_workers=0):
-    """Run `nsteps` config-2 steps on the CPU with the reference itself
+    """Run `nsteps` two-layer nx=256 steps on the CPU with the reference itself
     (kind 'reference': pyqg's unchanged QGModel and _step_forward over its
     compiled kernel, `threads` OpenMP threads for the kernel's loops,
     `fft_workers` > 0 for multithreaded transforms) or the numpy oracle
@@ -177,14 +177,14 @@ def cpu_model_steps(nsteps, nx=256, dt=3600.0, seed=0, threads=None, fft_workers
     from pyqg_gb300.model import grid_constants, spectral_filter
     from pyqg_gb300.qg_model import qg_inversion_matrix
     threads = threads or 1
-    g = grid_constants(nx, nx, C2["L"], C2["L"])
-    F1 = C2["rd"] ** -2 / (1. + C2["delta"])
-    F2 = C2["delta"] * F1
+    g = grid_constants(nx, nx, TWO_LAYER["L"], TWO_LAYER["L"])
+    F1 = TWO_LAYER["rd"] ** -2 / (1. + TWO_LAYER["delta"])
+    F2 = TWO_LAYER["delta"] * F1
     a = qg_inversion_matrix(g["wv2"], F1, F2)
-    filtr = spectral_filter(g["k"], g["l"], g["dx"], g["dy"], C2["filterfac"])
-    Qy = np.array([C2["beta"] + F1 * (C2["U1"] - C2["U2"]),
-                   C2["beta"] - F2 * (C2["U1"] - C2["U2"])])
-    Ubg = np.array([C2["U1"], C2["U2"]])
+    filtr = spectral_filter(g["k"], g["l"], g["dx"], g["dy"], TWO_LAYER["filterfac"])
+    Qy = np.array([TWO_LAYER["beta"] + F1 * (TWO_LAYER["U1"] - TWO_LAYER["U2"]),
+                   TWO_LAYER["beta"] - F2 * (TWO_LAYER["U1"] - TWO_LAYER["U2"])])
+    Ubg = np.array([TWO_LAYER["U1"], TWO_LAYER["U2"]])
     q0 = 1e-7 * np.random.default_rng(seed).standard_normal((2, nx, nx))
     try:
         import build_ref
@@ -205,7 +205,7 @@ def cpu_model_steps(nsteps, nx=256, dt=3600.0, seed=0, threads=None, fft_workers
             import warnings
             with warnings.catch_warnings():
                 warnings.simplefilter("ignore")
-                m = ref.QGModel(nx=nx, dt=dt, ntd=threads, **C2, **QUIET)
+                m = ref.QGModel(nx=nx, dt=dt, ntd=threads, **TWO_LAYER, **QUIET)
             m.q = q0
             step = m._step_forward
             kind = "reference"
@@ -219,13 +219,13 @@ def cpu_model_steps(nsteps, nx=256, dt=3600.0, seed=0, threads=None, fft_workers
             k.Ubg = Ubg
             k.Qy = Qy
             k.filtr = filtr
-            k.rek = C2["rek"]
+            k.rek = TWO_LAYER["rek"]
             k.dt = dt
             k.q = q0
             step = lambda: (k._invert(), k._do_advection(), k._do_friction(), k._forward_timestep())
             kind = "reference"
     except Exception:
-        o = O.OracleKernel(2, nx, nx, a, g["kk"], g["ll"], Ubg, Qy, filtr, C2["rek"], dt)
+        o = O.OracleKernel(2, nx, nx, a, g["kk"], g["ll"], Ubg, Qy, filtr, TWO_LAYER["rek"], dt)
         o.set_q(q0)
         step = o.step
         kind = "port"
@@ -271,7 +271,7 @@ def cpu_baseline(dt, sample_steps):
     secs, kind, cores = cpu_model_steps(sample_steps, dt=dt, threads=th, fft_workers=fw)
     return {"value": sim_yr_per_hr(sample_steps, dt, secs), "unit": "sim-yr/hr",
             "cores": cores, "kind": kind,
-            "sample": "%d config-2 steps (nx=256, FP64) on the host through pyqg's own QGModel._step_forward "
+            "sample": "%d two-layer steps (nx=256, dt=3600, FP64) on the host through pyqg's own QGModel._step_forward "
                       "over its compiled kernel, %.1f ms/step (%s, the fastest of "
                       "1 thread / all cores / multithreaded FFT)"
                       % (sample_steps, 1e3 * secs / sample_steps, cpu_variant_name(th, fw))}
@@ -295,11 +295,11 @@ def run_reference(args, rank, world):
             "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (config-2 physics), "
+            "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (standard two-layer physics), "
                                    "%d model steps per timed step" % sample,
                        "model_steps_per_step": sample, "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": value, "unit": "sim-yr/hr", "cores": cores, "kind": kind,
-                             "sample": "%d x %d config-2 steps through pyqg's own QGModel._step_forward "
+                             "sample": "%d x %d two-layer nx=256 steps through pyqg's own QGModel._step_forward "
                                        "over its compiled kernel (%s)"
                                        % (args.steps, sample, cpu_variant_name(th, fw))},
             "e2e": {"value": value, "unit": "sim-yr/hr", "h2d_bytes_per_step": 0,
@@ -343,7 +343,7 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     nx, dt = args.nx, 3600.0
-    m = P.QGModel(nx=nx, dt=dt, **C2, **QUIET)
+    m = P.QGModel(nx=nx, dt=dt, **TWO_LAYER, **QUIET)
     q0 = 1e-7 * np.random.default_rng(1000 + rank).standard_normal((2, nx, nx))
     m.q = q0
     stream = torch.cuda.current_stream(dev)
@@ -470,7 +470,7 @@ def run_ours(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if engine == "fp64" else "f64+int64",
         "data": "synthetic (seeded 1e-7 N(0,1) initial PV)",
-        "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (config-2 physics), "
+        "config": {"workload": "two-layer QG nx=ny=256 dt=3600 FP64 (standard two-layer physics), "
                                "%d model steps per timed step" % args.chunk,
                    "engine": engine if engine == "fp64" else
                    "fixed (FP64 state and pointwise physics; transforms in 64-bit block fixed point)",
@@ -514,7 +514,7 @@ def run_ours(args, rank, world, local_rank):
 
 
 def closure_throughput(args, plain_value, plain_fp64_transforms=None):
-    """Config-5 workload: two-layer nx=64 FP32 members with the 8-layer
+    """Closure workload: two-layer nx=64 FP32 members with the 8-layer
     convolutional closure applied every step (and the same ensemble without
     it), aggregate simulated years per wall-clock hour over the members.
     The network is randomly initialised: its cost does not depend on the
@@ -579,7 +579,7 @@ def closure_throughput(args, plain_value, plain_fp64_transforms=None):
     # default engine above transforms in 64-bit fixed point)
     res["vs_nx256_plain_fp64_transforms"] = (res["closure"]["value"] / plain_fp64_transforms
                                              if plain_fp64_transforms else None)
-    # config 5's own baseline: a 16-member FP64 nx=256 plain ensemble
+    # the closure's plain baseline: a 16-member FP64 nx=256 plain ensemble
     base = nx256_ensemble16(args)
     res["nx256_fp64_ensemble16"] = base
     agg = base["value"]
@@ -593,8 +593,8 @@ def closure_throughput(args, plain_value, plain_fp64_transforms=None):
 
 
 def nx256_ensemble16(args, nmembers=16):
-    """Aggregate sim-yr/hr of 16 FP64 nx=256 two-layer plain members (config-2
-    physics, dt = 3600 s), the faster of two ways of running them on one GPU:
+    """Aggregate sim-yr/hr of 16 FP64 nx=256 two-layer plain members (standard
+    two-layer physics, dt = 3600 s), the faster of two ways of running them on one GPU:
     the batched FP64 ensemble (FP64 transforms, one launch pair per step for
     all members) and 16 independent single models, each with the fused step
     of the default engine on its own stream (their kernels overlap)."""
@@ -605,7 +605,7 @@ def nx256_ensemble16(args, nmembers=16):
     rng = np.random.default_rng(4000)
     qs = [1e-7 * rng.standard_normal((2, 256, 256)) for _ in range(nmembers)]
     stream = torch.cuda.current_stream()
-    out = {"workload": "%d two-layer QG members nx=256 dt=3600 FP64 (config-2 physics), no closure"
+    out = {"workload": "%d two-layer QG members nx=256 dt=3600 FP64 (standard two-layer physics), no closure"
                        % nmembers}
     # (a) batched FP64 ensemble
     ens = P.Ensemble([("qg", dict(nx=256, dt=dt, **PHYSICS))] * nmembers, precision="fp64")
@@ -652,8 +652,8 @@ def nx256_ensemble16(args, nmembers=16):
     return out
 
 
-def config3_ensemble(rng):
-    """The config-3 members (614 x nx=64, 307 x nx=128, 103 x nx=256; 20 %
+def mixed_ensemble_1024(rng):
+    """The 1024 mixed-size members (614 x nx=64, 307 x nx=128, 103 x nx=256; 20 %
     three-layer; beta and rek drawn per member) as an FP32 Ensemble with
     seeded initial PV."""
     import pyqg_gb300 as P
@@ -675,12 +675,12 @@ def config3_ensemble(rng):
 
 
 def ensemble_throughput(args):
-    """Config-3 workload: 1024 FP32 members of uneven size, autotuned launch
+    """Mixed-size ensemble workload: 1024 FP32 members of uneven size, autotuned launch
     shapes, groups on concurrent branches and steady-state stretches
     replayed as CUDA graphs."""
     import torch
     rng = np.random.default_rng(1234)
-    ens, members = config3_ensemble(rng)
+    ens, members = mixed_ensemble_1024(rng)
     ens.step(4)
     ens.autotune()
     stream = torch.cuda.current_stream()
@@ -698,8 +698,8 @@ def ensemble_throughput(args):
     nbytes = 40 * S + 8 * Pn
     hbm, kind = peaks()
     ach = nbytes / (ms * 1e-3) / 1e9
-    traffic, traffic_src = stored_traffic("ensemble_config3_step")
-    return {"workload": "config 3: 1024 FP32 members (614 x nx=64, 307 x nx=128, 103 x nx=256, "
+    traffic, traffic_src = stored_traffic("ensemble_1024_mixed_step")
+    return {"workload": "1024 FP32 members (614 x nx=64, 307 x nx=128, 103 x nx=256, "
                         "20 % three-layer), uneven beta / rek, autotuned, CUDA graphs",
             "ms_per_ensemble_step": ms, "member_steps_per_s": len(members) / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
@@ -714,11 +714,11 @@ def profile_case(args):
     import torch
     import pyqg_gb300 as P
     if args.profile_step:
-        m = P.QGModel(nx=args.nx, dt=3600.0, **C2, **QUIET)
+        m = P.QGModel(nx=args.nx, dt=3600.0, **TWO_LAYER, **QUIET)
         m.q = 1e-7 * np.random.default_rng(0).standard_normal((2, args.nx, args.nx))
         m._step_fused(args.profile_step)
     if args.profile_ensemble:
-        ens, _ = config3_ensemble(np.random.default_rng(1234))
+        ens, _ = mixed_ensemble_1024(np.random.default_rng(1234))
         ens.step(4)
         ens.autotune()
         torch.cuda.synchronize()
@@ -750,14 +750,14 @@ def main():
     ap.add_argument("--closure-steps", type=int, default=5)
     ap.add_argument("--closure-chunk", type=int, default=100)
     ap.add_argument("--no-closure", action="store_true", help="skip the closure-ensemble measurement")
-    ap.add_argument("--no-ensemble", action="store_true", help="skip the config-3 ensemble measurement")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 1024-member mixed-size ensemble measurement")
     ap.add_argument("--ensemble-steps", type=int, default=200)
     ap.add_argument("--profile-step", type=int, default=0, metavar="N",
                     help="only run N fused nx=256 steps (a small case for profilers) and exit")
     ap.add_argument("--profile-cnn", type=int, default=0, metavar="B",
                     help="only run two closure-network forwards of a batch of B and exit")
     ap.add_argument("--profile-ensemble", type=int, default=0, metavar="N",
-                    help="only run N steps of the config-3 FP32 ensemble and exit")
+                    help="only run N steps of the 1024-member mixed-size FP32 ensemble and exit")
     args = ap.parse_args()
     if args.profile_step or args.profile_cnn or args.profile_ensemble:
         profile_case(args)

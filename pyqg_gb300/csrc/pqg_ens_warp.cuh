@@ -152,7 +152,8 @@ __device__ __forceinline__ void r2c_out(const float2 (&Z)[8], float2* X, int sx,
 // groups read and write their own row of the tile.  STAGE needs RB | ny.
 // ---------------------------------------------------------------------------
 // Register caps: 64 for the staged kernel (spills of 20-52 bytes at
-// M = 64, 128; config 3 0.66 against 0.68 ms with 85), 128 otherwise;
+// M = 64, 128; the 1024-member mixed ensemble steps in 0.66
+// against 0.68 ms with 85), 128 otherwise;
 // both measured faster than the compiler's unbounded choice (up to 125).
 template <int LOGM, bool STAGE>
 __global__ void __launch_bounds__(256, STAGE ? 4 : 2) e_row_w(EGeo g, EConsts<float> c, float2* scratch, const float* qphys,

@@ -1,4 +1,4 @@
-"""The FP32 form against the FP64 step (config 2: two-layer QG, nx=256,
+"""The FP32 form against the FP64 step (two-layer QG, nx=256,
 dt=3600 s).
 
 No counterpart in the reference.  From FP64 states spun up from seeded

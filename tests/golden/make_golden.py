@@ -70,16 +70,16 @@ def main(only=None):
     rng = np.random.default_rng
     files = {}
 
-    # Config-1 two-layer physics at nx=64 (seed 0), 100 steps.
-    c1 = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+    # Standard two-layer physics at nx=64, dt=7200 (seed 0), 100 steps.
+    two_layer = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
               U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
-    m = pyqg.QGModel(**c1, **QUIET)
+    m = pyqg.QGModel(**two_layer, **QUIET)
     q0 = 1e-7 * rng(0).standard_normal((2, 64, 64))
-    files["qg_c1_nx64.npz"] = run_case(m, q0, [1, 10, 100])
+    files["qg_two_layer_nx64.npz"] = run_case(m, q0, [1, 10, 100])
 
-    # Config-2 physics at nx=256, dt=3600 (seed 0): checksums only (size).
-    c2 = dict(c1, nx=256, dt=3600.0)
-    m = pyqg.QGModel(**c2, **QUIET)
+    # Standard two-layer physics at nx=256, dt=3600 (seed 0): checksums only (size).
+    two_layer_nx256 = dict(two_layer, nx=256, dt=3600.0)
+    m = pyqg.QGModel(**two_layer_nx256, **QUIET)
     q0 = 1e-7 * rng(0).standard_normal((2, 256, 256))
     m.q = q0
     idx = rng(7).integers(0, 256, size=(64, 2))
@@ -91,7 +91,7 @@ def main(only=None):
             rec["q%d_layer_l2" % s] = np.sqrt((q ** 2).sum(axis=(-2, -1)))
             rec["q%d_layer_sum" % s] = q.sum(axis=(-2, -1))
             rec["q%d_sample" % s] = q[:, idx[:, 0], idx[:, 1]].copy()
-    files["qg_c2_nx256_checksums.npz"] = rec
+    files["qg_two_layer_nx256_checksums.npz"] = rec
 
     # Three-layer LayeredModel (the ensemble's nz=3 physics) at nx=32.
     lay = dict(nz=3, nx=32, H=[500., 1000., 2500.], U=[0.05, 0.02, 0.0],
@@ -113,7 +113,7 @@ def main(only=None):
     dq = 1e-13 * rng(4).standard_normal((2, 32, 32))
     du = 1e-9 * rng(5).standard_normal((2, 32, 32))
     dv = 1e-9 * rng(6).standard_normal((2, 32, 32))
-    cp = dict(c1, nx=32)
+    cp = dict(two_layer, nx=32)
     m = pyqg.QGModel(**cp, q_parameterization=lambda m: dq,
                      uv_parameterization=lambda m: (du, dv), **QUIET)
     q0 = 1e-7 * rng(8).standard_normal((2, 32, 32))
@@ -163,11 +163,11 @@ def save(files, only=None):
 def physical_parameterizations(pyqg):
     """The reference's Smagorinsky, BackscatterBiharmonic, ZannaBolton2020
     and RingForcing (pyqg/parameterizations.py:132-366) evaluated on a
-    seeded state of config-1 physics at nx=32 after 10 steps, with u, v and ph refreshed from
+    seeded state of standard two-layer physics at nx=32 after 10 steps, with u, v and ph refreshed from
     that state by one inversion."""
-    c1 = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+    two_layer = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
               U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
-    m = pyqg.QGModel(**dict(c1, nx=32), **QUIET)
+    m = pyqg.QGModel(**dict(two_layer, nx=32), **QUIET)
     m.q = 1e-6 * np.random.default_rng(3).standard_normal((2, 32, 32))
     for _ in range(10):
         m._step_forward()
@@ -209,16 +209,16 @@ def diagnostics(pyqg):
     (get_diagnostic) with their sample counts.  The layered model's modal
     diagnostics need the numpy-1 reading of ``modal_projection``."""
     pyqg.Model.modal_projection = _numpy1_modal_projection
-    c1 = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+    two_layer = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
               U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
     lay = dict(nz=3, nx=32, H=[500., 1000., 2500.], U=[0.05, 0.02, 0.0],
                V=[0., 0., 0.], rek=5.787e-7, dt=7200.0)
     cases = {
-        "diag_qg_nx64.npz": (pyqg.QGModel, c1, {}, 11, 6),
+        "diag_qg_nx64.npz": (pyqg.QGModel, two_layer, {}, 11, 6),
         "diag_layered_nz3_nx32.npz": (pyqg.LayeredModel, lay, {}, 12, 6),
-        "diag_qg_smag_nx32.npz": (pyqg.QGModel, dict(c1, nx=32),
+        "diag_qg_smag_nx32.npz": (pyqg.QGModel, dict(two_layer, nx=32),
                                   dict(uv_parameterization=pyqg.Smagorinsky()), 13, 5),
-        "diag_qg_back_nx32.npz": (pyqg.QGModel, dict(c1, nx=32),
+        "diag_qg_back_nx32.npz": (pyqg.QGModel, dict(two_layer, nx=32),
                                   dict(q_parameterization=pyqg.BackscatterBiharmonic()), 14, 5),
     }
     out = {}
@@ -269,9 +269,9 @@ def dataset(pyqg):
     sys.modules.pop("pyqg.xarray_output", None)
     try:
         import pyqg.xarray_output as xo
-        c1 = dict(nx=32, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+        two_layer = dict(nx=32, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
                   U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
-        m = pyqg.QGModel(**c1, tavestart=0.0, taveint=7200.0, log_level=0)
+        m = pyqg.QGModel(**two_layer, tavestart=0.0, taveint=7200.0, log_level=0)
         m.q = 1e-6 * np.random.default_rng(15).standard_normal((2, 32, 32))
         q0 = np.asarray(m.q).copy()
         for _ in range(4):

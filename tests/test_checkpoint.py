@@ -5,7 +5,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-C1 = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
+TWO_LAYER = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
           U2=0.0, rek=5.787e-7, filterfac=23.6)
 QUIET = dict(tavestart=1e30, taveint=1e30, log_level=0)
 
@@ -14,7 +14,7 @@ QUIET = dict(tavestart=1e30, taveint=1e30, log_level=0)
 def test_resume_is_bit_exact(tmp_path, engine):
     import pyqg_gb300 as P
     q0 = 1e-7 * np.random.default_rng(3).standard_normal((2, 64, 64))
-    a = P.QGModel(nx=64, dt=7200.0, tmax=40 * 7200.0, **C1, **QUIET)
+    a = P.QGModel(nx=64, dt=7200.0, tmax=40 * 7200.0, **TWO_LAYER, **QUIET)
     a.engine = engine
     a.q = q0
     a.run()
@@ -22,7 +22,7 @@ def test_resume_is_bit_exact(tmp_path, engine):
     a.save_checkpoint(path)
     a.tmax = 90 * 7200.0
     a.run()
-    b = P.QGModel(nx=64, dt=7200.0, tmax=90 * 7200.0, **C1, **QUIET)
+    b = P.QGModel(nx=64, dt=7200.0, tmax=90 * 7200.0, **TWO_LAYER, **QUIET)
     b.load_checkpoint(path)
     assert (b.t, b.tc, b.ablevel, b.engine) == (40 * 7200.0, 40, 2, engine)
     b.run()

@@ -122,9 +122,9 @@ def test_gpu_dataset_matches_reference():
     import pyqg_gb300 as P
     from pyqg_gb300.xarray_output import model_to_dataset_spec
     g, meta = _fixture()
-    c1 = dict(nx=32, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025, U2=0.0,
+    two_layer = dict(nx=32, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025, U2=0.0,
               rek=5.787e-7, dt=7200.0, filterfac=23.6)
-    m = P.QGModel(**c1, tavestart=0.0, taveint=7200.0, log_level=0)
+    m = P.QGModel(**two_layer, tavestart=0.0, taveint=7200.0, log_level=0)
     m.q = g["q0"].copy()
     for _ in range(int(g["nsteps"])):
         m._step_forward()

@@ -17,7 +17,7 @@ import pytest
 from conftest import golden, rel_l2
 
 QUIET = dict(tavestart=1e30, taveint=1e30, log_level=0)
-C1 = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
+TWO_LAYER = dict(nx=64, L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500,
           U1=0.025, U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
 
 
@@ -79,10 +79,10 @@ def _set_state(m, g):
 
 
 @pytest.mark.gpu
-def test_unchanged_reference_qgmodel_config1_100_steps(ref_on_gpu_kernel):
+def test_unchanged_reference_qgmodel_nx64_100_steps(ref_on_gpu_kernel):
     pyqg = ref_on_gpu_kernel
-    g = golden("qg_c1_nx64.npz")
-    m = pyqg.QGModel(**C1, tmax=100 * C1["dt"], **QUIET)
+    g = golden("qg_two_layer_nx64.npz")
+    m = pyqg.QGModel(**TWO_LAYER, tmax=100 * TWO_LAYER["dt"], **QUIET)
     assert rel_l2(m.filtr, g["filtr"]) < 1e-12
     assert rel_l2(np.asarray(m.a).real, g["a"]) < 1e-13
     _set_state(m, g)
@@ -96,8 +96,8 @@ def test_unchanged_reference_qgmodel_stage_by_stage(ref_on_gpu_kernel):
     """The reference's _step_forward drives the kernel's stage methods; the
     intermediate fields after one step equal the reference's."""
     pyqg = ref_on_gpu_kernel
-    g = golden("qg_c1_nx64.npz")
-    m = pyqg.QGModel(**C1, **QUIET)
+    g = golden("qg_two_layer_nx64.npz")
+    m = pyqg.QGModel(**TWO_LAYER, **QUIET)
     _set_state(m, g)
     m._invert()
     assert rel_l2(m.ph, g["s1_ph"]) < 1e-13
@@ -140,7 +140,7 @@ def test_unchanged_reference_model_with_hooks(ref_on_gpu_kernel):
     pyqg = ref_on_gpu_kernel
     g = golden("qg_params_nx32.npz")
     dq, du, dv = g["param_dq"], g["param_du"], g["param_dv"]
-    m = pyqg.QGModel(**dict(C1, nx=32), q_parameterization=lambda m: dq,
+    m = pyqg.QGModel(**dict(TWO_LAYER, nx=32), q_parameterization=lambda m: dq,
                      uv_parameterization=lambda m: (du, dv), **QUIET)
     _set_state(m, g)
     for _ in range(5):

@@ -11,7 +11,7 @@ from conftest import golden, rel_l2
 
 pytestmark = pytest.mark.gpu
 
-C1 = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
+TWO_LAYER = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
           U2=0.0, rek=5.787e-7, filterfac=23.6)
 TOL_STAGE = 1e-13
 TOL_100 = 1e-12
@@ -62,8 +62,8 @@ def test_transforms_match_numpy(P, quiet, n):
 
 
 def test_stage_by_stage_step1(P, quiet):
-    g = golden("qg_c1_nx64.npz")
-    m = P.QGModel(nx=64, dt=7200.0, **C1, **quiet)
+    g = golden("qg_two_layer_nx64.npz")
+    m = P.QGModel(nx=64, dt=7200.0, **TWO_LAYER, **quiet)
     m.q = g["q0"]
     m._invert()
     assert rel_l2(m.ph, g["s1_ph"]) < TOL_STAGE
@@ -79,10 +79,10 @@ def test_stage_by_stage_step1(P, quiet):
     assert rel_l2(m.q, g["q_1"]) < TOL_STAGE
 
 
-def test_100_steps_config1(P, quiet):
-    """Config-1 physics (nx=64, dt=7200): 1e-12 gate after 100 steps."""
-    g = golden("qg_c1_nx64.npz")
-    m = P.QGModel(nx=64, dt=7200.0, tmax=100 * 7200.0, **C1, **quiet)
+def test_100_steps_nx64(P, quiet):
+    """Standard two-layer physics (nx=64, dt=7200): 1e-12 gate after 100 steps."""
+    g = golden("qg_two_layer_nx64.npz")
+    m = P.QGModel(nx=64, dt=7200.0, tmax=100 * 7200.0, **TWO_LAYER, **quiet)
     m.q = g["q0"]
     m._step_forward()
     assert rel_l2(m.q, g["q_1"]) < TOL_STAGE
@@ -98,8 +98,8 @@ def test_100_steps_config1(P, quiet):
 def test_fused_is_bit_identical_to_staged(P, quiet, engine):
     rng = np.random.default_rng(5)
     q0 = 1e-7 * rng.standard_normal((2, 64, 64))
-    a = P.QGModel(nx=64, dt=7200.0, **C1, **quiet)
-    b = P.QGModel(nx=64, dt=7200.0, **C1, **quiet)
+    a = P.QGModel(nx=64, dt=7200.0, **TWO_LAYER, **quiet)
+    b = P.QGModel(nx=64, dt=7200.0, **TWO_LAYER, **quiet)
     a.engine = b.engine = engine
     a.q = q0
     b.q = q0
@@ -112,13 +112,13 @@ def test_fused_is_bit_identical_to_staged(P, quiet, engine):
     assert (a.t, a.tc, a.ablevel) == (b.t, b.tc, b.ablevel)
 
 
-def test_config2_nx256_vs_oracle(P, quiet):
-    """Config-2 physics (nx=256, dt=3600): golden checksums after 1 and 10
+def test_nx256_vs_oracle(P, quiet):
+    """Standard two-layer physics (nx=256, dt=3600): golden checksums after 1 and 10
     steps, then the CPU oracle after 100 steps (1e-12 gate)."""
     import pyqg_oracle as O
-    g = golden("qg_c2_nx256_checksums.npz")
+    g = golden("qg_two_layer_nx256_checksums.npz")
     q0 = 1e-7 * np.random.default_rng(0).standard_normal((2, 256, 256))
-    m = P.QGModel(nx=256, dt=3600.0, tmax=100 * 3600.0, **C1, **quiet)
+    m = P.QGModel(nx=256, dt=3600.0, tmax=100 * 3600.0, **TWO_LAYER, **quiet)
     m.q = q0
     idx = g["sample_idx"]
     for s in range(1, 11):
@@ -169,7 +169,7 @@ def test_model_families_vs_reference(P, quiet, case):
 def test_parameterization_hooks_vs_reference(P, quiet):
     g = golden("qg_params_nx32.npz")
     dq, du, dv = g["param_dq"], g["param_du"], g["param_dv"]
-    m = P.QGModel(nx=32, dt=7200.0, **C1, q_parameterization=lambda m: dq,
+    m = P.QGModel(nx=32, dt=7200.0, **TWO_LAYER, q_parameterization=lambda m: dq,
                   uv_parameterization=lambda m: (du, dv), **quiet)
     m.q = g["q0"]
     m._step_forward()
@@ -194,16 +194,16 @@ def test_layered_fixture_inversion(P):
 @pytest.mark.parametrize("engine", ["fp64", "fixed"])
 def test_engines_100_steps(P, quiet, engine):
     """Both transform engines of the fused step pass the 1e-12 gate, at
-    config-1 (vs the reference) and config-2 (vs the oracle) physics."""
+    nx=64 (vs the reference) and nx=256 (vs the oracle)."""
     import pyqg_oracle as O
-    g = golden("qg_c1_nx64.npz")
-    m = P.QGModel(nx=64, dt=7200.0, tmax=100 * 7200.0, **C1, **quiet)
+    g = golden("qg_two_layer_nx64.npz")
+    m = P.QGModel(nx=64, dt=7200.0, tmax=100 * 7200.0, **TWO_LAYER, **quiet)
     m.engine = engine
     m.q = g["q0"]
     m.run()
     assert rel_l2(m.q, g["q_100"]) < TOL_100
     q0 = 1e-7 * np.random.default_rng(1).standard_normal((2, 256, 256))
-    m = P.QGModel(nx=256, dt=3600.0, tmax=100 * 3600.0, **C1, **quiet)
+    m = P.QGModel(nx=256, dt=3600.0, tmax=100 * 3600.0, **TWO_LAYER, **quiet)
     m.engine = engine
     m.q = q0
     m.run()
@@ -219,7 +219,7 @@ def test_fixed_engine_extreme_magnitudes(P, quiet):
     amplitude the dynamics survives step like the FP64 engine, and a zero
     field stays exactly zero."""
     rng = np.random.default_rng(9)
-    m = P.QGModel(nx=64, dt=7200.0, tmax=5 * 7200.0, **C1, **quiet)
+    m = P.QGModel(nx=64, dt=7200.0, tmax=5 * 7200.0, **TWO_LAYER, **quiet)
     m.engine = "fixed"
     m.q = np.zeros((2, 64, 64))
     m.run()
@@ -228,7 +228,7 @@ def test_fixed_engine_extreme_magnitudes(P, quiet):
         q0 = scale * rng.standard_normal((2, 64, 64))
         res = {}
         for engine in ("fp64", "fixed"):
-            m = P.QGModel(nx=64, dt=7200.0, tmax=20 * 7200.0, **C1, **quiet)
+            m = P.QGModel(nx=64, dt=7200.0, tmax=20 * 7200.0, **TWO_LAYER, **quiet)
             m.engine = engine
             m.q = q0
             m.run()
@@ -258,23 +258,23 @@ def test_non_square_kernel_vs_oracle(P, nx, ny, engines):
     kk = 2 * np.pi / L * np.arange(nx // 2 + 1)
     ll = 2 * np.pi / W * np.append(np.arange(0., ny / 2), np.arange(-ny / 2, 0.))
     k, l = np.meshgrid(kk, ll)
-    F1 = C1["rd"] ** -2 / (1. + C1["delta"])
-    F2 = C1["delta"] * F1
+    F1 = TWO_LAYER["rd"] ** -2 / (1. + TWO_LAYER["delta"])
+    F2 = TWO_LAYER["delta"] * F1
     a = qg_inversion_matrix(k ** 2 + l ** 2, F1, F2)
-    filtr = spectral_filter(k, l, L / nx, W / ny, C1["filterfac"])
-    Ubg = np.array([C1["U1"], C1["U2"]])
-    Qy = np.array([C1["beta"] + F1 * (C1["U1"] - C1["U2"]), C1["beta"] - F2 * (C1["U1"] - C1["U2"])])
+    filtr = spectral_filter(k, l, L / nx, W / ny, TWO_LAYER["filterfac"])
+    Ubg = np.array([TWO_LAYER["U1"], TWO_LAYER["U2"]])
+    Qy = np.array([TWO_LAYER["beta"] + F1 * (TWO_LAYER["U1"] - TWO_LAYER["U2"]), TWO_LAYER["beta"] - F2 * (TWO_LAYER["U1"] - TWO_LAYER["U2"])])
     q0 = 1e-7 * np.random.default_rng(12).standard_normal((2, ny, nx))
 
     def kernel(engine):
         kn = PseudoSpectralKernel(2, ny, nx)
         kn.kk, kn.ll, kn.a, kn.Ubg, kn.Qy = kk, ll, a, Ubg, Qy
-        kn.filtr, kn.rek, kn.dt = filtr, C1["rek"], 7200.0
+        kn.filtr, kn.rek, kn.dt = filtr, TWO_LAYER["rek"], 7200.0
         kn.engine = engine
         kn.q = q0
         return kn
 
-    o = O.OracleKernel(2, ny, nx, a, kk, ll, Ubg, Qy, filtr, C1["rek"], 7200.0)
+    o = O.OracleKernel(2, ny, nx, a, kk, ll, Ubg, Qy, filtr, TWO_LAYER["rek"], 7200.0)
     o.set_q(q0)
     for _ in range(30):
         o.step()

@@ -68,7 +68,7 @@ def _qg_consts(n, L=1e6, rd=15000.0, delta=0.25, beta=1.5e-11, U1=0.025,
 
 
 def test_qg_constants_equal_reference():
-    g = golden("qg_c1_nx64.npz")
+    g = golden("qg_two_layer_nx64.npz")
     c = _qg_consts(64)
     for k in ("a", "kk", "ll", "Qy"):
         np.testing.assert_array_equal(c[k], g[k], err_msg=k)

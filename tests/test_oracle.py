@@ -16,7 +16,7 @@ def oracle_from(g, nz, n, q_param=None, uv_param=None):
 
 
 @pytest.mark.parametrize("case,nz,n,steps", [
-    ("qg_c1_nx64.npz", 2, 64, (1, 10, 100)),
+    ("qg_two_layer_nx64.npz", 2, 64, (1, 10, 100)),
     ("layered_nz3_nx32.npz", 3, 32, (1, 20)),
     ("bt_nx32.npz", 1, 32, (1, 20)),
     ("sqg_nx32.npz", 1, 32, (1, 20)),
@@ -36,7 +36,7 @@ def test_oracle_bit_identical_to_reference(case, nz, n, steps):
 
 
 def test_oracle_stages_step1():
-    g = golden("qg_c1_nx64.npz")
+    g = golden("qg_two_layer_nx64.npz")
     o = oracle_from(g, 2, 64)
     o.invert()
     np.testing.assert_array_equal(o.ph, g["s1_ph"])
@@ -62,8 +62,8 @@ def test_oracle_parameterization_hooks():
             np.testing.assert_array_equal(o.q, g["q_%d" % s])
 
 
-def test_oracle_config2_checksums():
-    g = golden("qg_c2_nx256_checksums.npz")
+def test_oracle_nx256_checksums():
+    g = golden("qg_two_layer_nx256_checksums.npz")
     c = O.qg_constants(256)
     o = O.OracleKernel(c["nz"], 256, 256, c["a"], c["kk"], c["ll"], c["Ubg"],
                        c["Qy"], c["filtr"], 5.787e-7, 3600.0)
@@ -90,7 +90,7 @@ def test_oracle_transform_conventions(n):
 def test_planted_mistake_is_detected():
     """A wrong sign in the drag (planted in a copy of the oracle) must fail
     the same comparison the real tests use."""
-    g = golden("qg_c1_nx64.npz")
+    g = golden("qg_two_layer_nx64.npz")
 
     class Broken(O.OracleKernel):
         def do_friction(self):
@@ -137,20 +137,20 @@ def test_reference_multithreaded_fft_variant_is_bit_identical():
     from pyqg_gb300.model import grid_constants, spectral_filter
     from pyqg_gb300.qg_model import qg_inversion_matrix
     mod = build_ref.load()
-    nx, C2 = 64, bench.C2
-    g = grid_constants(nx, nx, C2["L"], C2["L"])
-    F1 = C2["rd"] ** -2 / (1. + C2["delta"])
-    F2 = C2["delta"] * F1
+    nx, phys = 64, bench.TWO_LAYER
+    g = grid_constants(nx, nx, phys["L"], phys["L"])
+    F1 = phys["rd"] ** -2 / (1. + phys["delta"])
+    F2 = phys["delta"] * F1
     q0 = 1e-7 * np.random.default_rng(4).standard_normal((2, nx, nx))
     out = []
     for workers in (0, 4):
         k = bench._ref_kernel(mod, workers)(2, nx, nx, 1, 0, 0)
         k.ll, k.kk = g["ll"], g["kk"]
         k.a = qg_inversion_matrix(g["wv2"], F1, F2)
-        k.Ubg = np.array([C2["U1"], C2["U2"]])
-        k.Qy = np.array([C2["beta"] + F1 * (C2["U1"] - C2["U2"]), C2["beta"] - F2 * (C2["U1"] - C2["U2"])])
-        k.filtr = spectral_filter(g["k"], g["l"], g["dx"], g["dy"], C2["filterfac"])
-        k.rek, k.dt = C2["rek"], 3600.0
+        k.Ubg = np.array([phys["U1"], phys["U2"]])
+        k.Qy = np.array([phys["beta"] + F1 * (phys["U1"] - phys["U2"]), phys["beta"] - F2 * (phys["U1"] - phys["U2"])])
+        k.filtr = spectral_filter(g["k"], g["l"], g["dx"], g["dy"], phys["filterfac"])
+        k.rek, k.dt = phys["rek"], 3600.0
         k.q = q0
         for _ in range(20):
             k._invert()

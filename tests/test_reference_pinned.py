@@ -4,7 +4,7 @@ reference package):
 
 * ``params_physical_nx32.npz``: Smagorinsky, BackscatterBiharmonic,
   ZannaBolton2020 and RingForcing (``pyqg/parameterizations.py:132-366``) on
-  a seeded config-1 state at nx=32;
+  a seeded two-layer state at nx=32;
 * ``diag_*.npz``: every registered diagnostic (time averages and counts,
   ``pyqg/model.py:802-814``) of short seeded runs of the two-layer and the
   three-layer model, and of runs with a uv and a q parameterization.
@@ -18,7 +18,7 @@ import pytest
 
 from conftest import golden
 
-C1 = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
+TWO_LAYER = dict(L=1e6, beta=1.5e-11, rd=15000.0, delta=0.25, H1=500, U1=0.025,
           U2=0.0, rek=5.787e-7, dt=7200.0, filterfac=23.6)
 PARAM_TOL = 1e-12
 DIAG_TOL = 1e-11
@@ -103,7 +103,7 @@ def test_host_restatement_of_parameterizations_matches_reference():
 
 
 def _gpu_model_at(P, g):
-    m = P.QGModel(nx=g["u"].shape[-1], **C1, tavestart=1e30, taveint=1e30, log_level=0)
+    m = P.QGModel(nx=g["u"].shape[-1], **TWO_LAYER, tavestart=1e30, taveint=1e30, log_level=0)
     m.q = g["q"].copy()
     m._invert()
     close(m.ph, g["ph"], 1e-13, "ph")
@@ -149,12 +149,12 @@ def test_gpu_diagnostics_match_reference(name):
                rek=5.787e-7, dt=7200.0)
     diag = dict(tavestart=0.0, taveint=7200.0, log_level=0)
     make = {
-        "diag_qg_nx64.npz": lambda: P.QGModel(nx=64, **C1, **diag),
+        "diag_qg_nx64.npz": lambda: P.QGModel(nx=64, **TWO_LAYER, **diag),
         "diag_layered_nz3_nx32.npz": lambda: P.LayeredModel(nx=32, **lay, **diag),
         "diag_qg_smag_nx32.npz": lambda: P.QGModel(nx=32, uv_parameterization=P.Smagorinsky(),
-                                                   **C1, **diag),
+                                                   **TWO_LAYER, **diag),
         "diag_qg_back_nx32.npz": lambda: P.QGModel(nx=32, q_parameterization=P.BackscatterBiharmonic(),
-                                                   **C1, **diag),
+                                                   **TWO_LAYER, **diag),
     }[name]
     m = make()
     assert m.gpu_diagnostics
