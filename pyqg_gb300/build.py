@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIBNAME = "libpyqg_gb300.so"
-ARCH = os.environ.get("PQG_CUDA_ARCH", "103a")
+ARCH = "103a"   # GB300 only: the kernels use tcgen05, TMA and sm_103a cluster features
 
 
 def nvcc_path():
