@@ -55,6 +55,32 @@ def test_product_refuses_to_run_without_gpu():
         P.QGModel()
 
 
+def test_parameterization_entry_points_refuse_bad_arguments():
+    """The pointwise parameterization stages check their arguments on the
+    host and report PQG_ERR_INVALID with the entry point's name before any
+    CUDA call (so this runs without a GPU)."""
+    from pyqg_gb300 import _lib
+    L = _lib.lib()
+    x = 8   # a non-null placeholder address: the checks reject the call first
+    cases = {
+        "pqg_smag_strain": (0, 8, 5, x, x, x, x, x, None),
+        "pqg_smag_stress": (2, 8, 8, x, 1.0, None, None, None),
+        "pqg_smag_divergence": (2, 8, 5, x, x, None, x, None),
+        "pqg_zb_gradients": (2, 0, 5, x, x, x, x, x, None),
+        "pqg_zb_products": (2, 8, 8, None, x, None),
+        "pqg_zb_combine": (2, 8, 5, x, x, x, 1.0, None, None),
+        "pqg_lap_power": (2, 8, 5, x, x, 3, 1.0, x, x, None),
+        "pqg_layer_mix": (9, 2, 64, x, x, x, None),
+        "pqg_mul_scaled": (0, x, 1.0, x, x, None),
+        "pqg_backscatter": (2, 8, 8, x, x, x, None, 1.0, 1e-32, x, x, None),
+        "pqg_ring_normalize": (1, 8, 8, x, None, 1.0, x, x, None),
+    }
+    for name, args in cases.items():
+        rc = getattr(L, name)(*args)
+        assert rc == _lib.PQG_ERR_INVALID, name
+        assert name in L.pqg_last_error().decode(), name
+
+
 def _qg_consts(n, L=1e6, rd=15000.0, delta=0.25, beta=1.5e-11, U1=0.025,
                U2=0.0, filterfac=23.6):
     from pyqg_gb300.model import grid_constants, spectral_filter
