@@ -257,8 +257,8 @@ int pqg_step_profile(pqg_plan *plan, pqg_state *state, int nsteps,
 int pqg_rfft2_noalloc(const double *x, double *xh, int nplanes, int ny,
                       int nx, void *stream);
 
-/* Inversion matrices built in FP64 on the device (the benchmark spec's
- * precision form builds its matrices here and rounds them once):
+/* Inversion matrices built in FP64 on the device (the FP32 precision form
+ * builds its matrices here and rounds them once):
  * a (nz, nz, nl, nk) = (S - kappa^2 I)^-1 per wavenumber, kappa^2 =
  * kk[k]^2 + ll[l]^2, 0 where singular (kappa = 0).  S is a HOST nz x nz
  * row-major array; kk (nk), ll (nl) and a are DEVICE arrays.

@@ -539,8 +539,12 @@ class Model(PseudoSpectralKernel):
             return ctypes.c_void_p(t.data_ptr())
 
         def mix(mat, x):
-            """sum_j mat[i][j] x[j] for (n, ...) device x."""
-            mat = np.ascontiguousarray(np.atleast_2d(np.asarray(mat, dtype=np.float64)))
+            """sum_j mat[i][j] x[j] for (n, ...) device x (the real part of a
+            complex-typed layer matrix, whose values are real)."""
+            mat = np.asarray(mat)
+            if np.iscomplexobj(mat):
+                mat = mat.real
+            mat = np.ascontiguousarray(np.atleast_2d(mat.astype(np.float64)))
             x = x.contiguous()
             plane = x[0].numel() * (2 if x.is_complex() else 1)
             out = torch.empty((mat.shape[0],) + tuple(x.shape[1:]), dtype=x.dtype, device=self._device)

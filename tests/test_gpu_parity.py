@@ -2,7 +2,7 @@
 the reference pyqg) and against the CPU oracle.
 
 Tolerances: FP64 transforms agree with numpy.fft/pocketfft to ~1e-15
-relative; the spec gate is relative L2 on q <= 1e-12 after 100 steps.
+relative; the parity gate is relative L2 on q <= 1e-12 after 100 steps.
 """
 import numpy as np
 import pytest
