@@ -17,6 +17,12 @@
  *     All compute calls are asynchronous on that stream.
  *   - Every function returns PQG_OK (0) or a PQG_ERR_* code; the message of
  *     the last error on the calling thread is returned by pqg_last_error().
+ *   - Threads: like pyqg's kernel object, a plan, an ensemble or a network
+ *     is not re-entrant: calls on one object must not overlap from several
+ *     host threads.  The ensemble step calls (pqg_ens_step_many,
+ *     pqg_ens_autotune, pqg_ens_set_constants) share one process-wide cache
+ *     of CUDA graphs, so ensembles are stepped from one host thread at a
+ *     time.
  *   - Transforms: pqg_rfft2 is unnormalised, pqg_irfft2 scales by 1/(nx ny)
  *     and ignores the imaginary parts of the k = 0 and k = nx/2 columns after
  *     the y transform, as numpy.fft.irfftn / FFTW c2r do.
