@@ -18,23 +18,24 @@
 // consumer wraps indices.  Master weights are FP32 w[co][tap][ci].
 //
 // Three convolution kernels:
-//  * k_conv_rows (64 input channels, at most 32 outputs): a tile is
-//    two full image rows, so every A operand window is aligned, and the five
-//    horizontal taps are folded into the MMA's N dimension (N = 5 x 32 for 32
-//    output channels); the epilogue sums the horizontally shifted columns.
-//    It replaces five N = 32 MMAs, bound by reading the A operand from shared
-//    memory, with one N = 160 MMA bound by the tensor pipe, at the price of
-//    a five times wider epilogue.
-//  * k_conv_halo (input channels a multiple of 16, the other layers): a CTA
-//    computes a tile of 16 rows x 8 SX columns.  TMA loads the input tile with its halo once into
+//  * k_conv_halo (16, 32, 64 or 128 channels along K): every forward layer
+//    (the network input is stored zero-padded to 16 channels) and the data
+//    gradients with at least 16 channels.  A CTA computes a tile of 16 rows
+//    x 8 SX columns.  TMA loads the input tile with its halo once into
 //    shared memory as one slab per 8 channels (pixel-major, 16 bytes per
 //    pixel); the A operand of tap (dy, dx) is then a shifted descriptor over
 //    the same slabs (core matrix = 8 consecutive pixels of a row, next
 //    8-pixel group = next image row).  The per-tap weight blocks stream
 //    through a bulk-copy ring of `nst` stages (all 25 taps resident when
 //    they fit); one thread per 8-column subtile issues its MMAs.
-//  * k_conv_gather (few input channels, e.g. the 2-channel input layer):
-//    threads gather a K-chunk of 64 (tap, channel) pairs per pixel.
+//  * k_conv_gather (few channels along K: the data gradient through the
+//    2-channel output layer): threads gather a K-chunk of 64 (tap, channel)
+//    pairs per pixel.
+//  * k_conv_rows (opt-in, PQG_CNN_ROWS; measured slower than the halo
+//    kernel on these layers): a tile is two full image rows, so every A
+//    operand window is aligned, and the five horizontal taps are folded into
+//    the MMA's N dimension (N = 5 x 32 for 32 output channels); the epilogue
+//    sums the horizontally shifted columns.
 // The weight gradient gathers (tap, channel) x pixel tiles (k_wgrad) and
 // adds its partial sums atomically.
 #include <cuda_runtime.h>
