@@ -9,13 +9,18 @@
 // one graph branch per group.
 //
 // Precision forms: FP32 state, transforms, products and Adams-Bashforth
-// update (`float2`), with the inversion matrix and constants built in FP64
-// on the host and rounded once, and the energy / enstrophy sums accumulated
-// in FP64; or FP64 throughout (`double2`), which reproduces the single-model
-// FP64 step bit for bit.
+// update (`float2`), with the inversion matrix built in FP64 (on the GPU,
+// pqg_inversion_matrix) and the constants rounded once, and the energy /
+// enstrophy sums accumulated in FP64; or FP64 throughout (`double2`), which
+// reproduces the single-model FP64 step bit for bit.  FP32 groups with
+// 16 <= nx, ny <= 256 and at most three layers run the warp-owned row and
+// column kernels of pqg_ens_warp.cuh; the others the block-wide kernels
+// below (or, where the autotuner picks it, one CTA per member).
 //
-// Layout (member-major): q (B, nz, ny, nx); qh and the tendencies
-// (B, nz, ny, nk); transposition scratch (B, 3 nz, ny, nk) (planes U, V, Q).
+// Layout (member-major, spectral planes k-major so that a column is
+// contiguous): q (B, nz, ny, nx); qh and the tendencies (B, nz, nk, ny);
+// transposition scratch (B, nfield nz, nk, ny) (planes U, V, Q, and F, the
+// closure's forcing, when a network is attached).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
