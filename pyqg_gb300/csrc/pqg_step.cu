@@ -17,6 +17,9 @@
 // The column kernel runs one CTA per (layer, column); the nz CTAs of a
 // column form a thread-block cluster and exchange the per-layer qh values
 // the layer coupling needs through distributed shared memory.
+// Transform engines (a plan setting): FP64 Stockham transforms, or, the
+// default on power-of-two grids, the same transforms in 64-bit block fixed
+// point (pqg_fixed.cuh).  The pointwise physics is FP64 under both.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
