@@ -253,3 +253,24 @@ def test_reference_arm_prints_its_json_line():
     assert set(line["cpu_baseline"]) >= {"value", "unit", "cores", "kind", "sample"}
     assert line["cpu_baseline"]["kind"] in ("reference", "port")
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+
+
+def test_bench_measurement_definitions():
+    """The bench's units: compulsory FP64 bytes per model step B64 = 80 S +
+    16 P (S spectral, P grid points; 468,992 B at nx=64 and 7,380,992 B at
+    nx=256 for two layers, 703,488 B and 11,071,488 B for three), a year of
+    360 days (pyqg/tests/test_reference_solns.py:12), and the stored ncu
+    traffic labelled with the capture that made it."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    assert bench.algorithmic_bytes(2, 64, 64) == 468992
+    assert bench.algorithmic_bytes(2, 256, 256) == 7380992
+    assert bench.algorithmic_bytes(3, 64, 64) == 703488
+    assert bench.algorithmic_bytes(3, 256, 256) == 11071488
+    # one year of dt = 3600 s steps in one hour of wall time is 1 sim-yr/hr
+    assert abs(bench.sim_yr_per_hr(360 * 24, 3600.0, 3600.0) - 1.0) < 1e-12
+    for name in ("k_col_fused_fx", "k_row_adv_fx", "ensemble_1024_mixed_step"):
+        nbytes, src = bench.stored_traffic(name)
+        assert nbytes > 0 and src.startswith("stored ncu capture: ncu ") and "--clock-control none" in src
