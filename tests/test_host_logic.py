@@ -274,3 +274,21 @@ def test_bench_measurement_definitions():
     for name in ("k_col_fused_fx", "k_row_adv_fx", "ensemble_1024_mixed_step"):
         nbytes, src = bench.stored_traffic(name)
         assert nbytes > 0 and src.startswith("stored ncu capture: ncu ") and "--clock-control none" in src
+
+
+def test_closure_experiment_truncation_matches_the_coarse_oracle():
+    """The experiment's host truncation of physical PV (used for the coarse
+    runs' initial states) is the coarse-graining oracle's sharp cutoff:
+    |k|, |l| < nc / 2 kept, amplitudes rescaled to the coarse grid."""
+    from coarse_oracle import truncate
+    from pyqg_oracle import irfft2, rfft2
+    from pyqg_gb300.closure_experiment import _truncate_physical
+    rng = np.random.default_rng(17)
+    for nf, nc in ((64, 32), (256, 64), (96, 32)):
+        q = rng.standard_normal((2, nf, nf))
+        got = _truncate_physical(q, nc)
+        want = irfft2(truncate(rfft2(q), nc, nc))
+        assert got.shape == (2, nc, nc)
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-13 * np.abs(want).max())
+        # idempotent: a truncated field is kept as it is
+        np.testing.assert_allclose(_truncate_physical(got, nc), got, rtol=0, atol=1e-13 * np.abs(got).max())
